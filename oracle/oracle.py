@@ -1,0 +1,177 @@
+"""ctypes front-end of the CPU oracle (``oracle/fteik_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: used by ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU legs of ``bench.py`` as the checker and the timed CPU baseline. The
+product package never imports this module.
+
+The functions mirror the reference's numba entry points
+(``fteikpy/_fteik/_fteik3d.py:516-525`` ``solve3d``,
+``fteikpy/_fteik/_fteik2d.py:667-674`` ``solve2d``, ``fteikpy/_interp/*``,
+``fteikpy/_fteik/_ray*.py``) and take/return NumPy arrays.
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfteik_oracle.so")
+
+_lib = None
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_L = ctypes.c_long
+_P = ctypes.c_void_p
+
+
+def build():
+    """Compile the oracle shared library (gcc, IEEE semantics, OpenMP)."""
+    subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
+            os.path.join(HERE, "fteik_oracle.c")
+        ):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oracle_fteik3d_many.argtypes = [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _I]
+        L.oracle_fteik3d_many.restype = _I
+        L.oracle_fteik2d_many.argtypes = [_P, _I, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _I]
+        L.oracle_fteik2d_many.restype = _I
+        L.oracle_interp3d.argtypes = [_P, _I, _P, _I, _P, _I, _P, _L, _P, _I, _D, _P]
+        L.oracle_interp2d.argtypes = [_P, _I, _P, _I, _P, _L, _P, _I, _D, _P]
+        L.oracle_vinterp3d.argtypes = [_P, _I, _P, _I, _P, _I, _P, _P, _I, _P, _D, _D, _P]
+        L.oracle_vinterp2d.argtypes = [_P, _I, _P, _I, _P, _P, _I, _P, _D, _D, _P]
+        L.oracle_ray3d.argtypes = [_P, _I, _P, _I, _P, _I, _P, _P, _I, _P, _D, _I, _I, _P, _P, _P]
+        L.oracle_ray2d.argtypes = [_P, _I, _P, _I, _P, _P, _I, _P, _D, _I, _I, _P, _P, _P]
+        _lib = L
+    return _lib
+
+
+def _c(a, dtype=np.float64):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def solve3d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
+    """Batched 3D solve. ``sources`` is (nsrc, 3), relative to the grid origin.
+
+    Returns (tt[nsrc, nz+1, nx+1, ny+1], ttgrad[nsrc, ..., 3] or None, vzero[nsrc]).
+    """
+    slow = _c(slow)
+    src = _c(np.atleast_2d(sources))
+    nz, nx, ny = slow.shape
+    nsrc = len(src)
+    tt = np.empty((nsrc, nz + 1, nx + 1, ny + 1))
+    tg = np.empty((nsrc, nz + 1, nx + 1, ny + 1, 3)) if grad else np.empty(1)
+    vz = np.empty(nsrc)
+    nthreads = nthreads or os.cpu_count()
+    st = lib().oracle_fteik3d_many(
+        _p(slow), nz, nx, ny, *map(float, gridsize), _p(src), nsrc, int(nsweep), int(grad),
+        _p(tt), _p(tg), _p(vz), int(nthreads),
+    )
+    if st == 1:
+        raise ValueError("source out of bound")
+    return tt, (tg if grad else None), vz
+
+
+def solve2d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
+    slow = _c(slow)
+    src = _c(np.atleast_2d(sources))
+    nz, nx = slow.shape
+    nsrc = len(src)
+    tt = np.empty((nsrc, nz + 1, nx + 1))
+    tg = np.empty((nsrc, nz + 1, nx + 1, 2)) if grad else np.empty(1)
+    vz = np.empty(nsrc)
+    nthreads = nthreads or os.cpu_count()
+    st = lib().oracle_fteik2d_many(
+        _p(slow), nz, nx, *map(float, gridsize), _p(src), nsrc, int(nsweep), int(grad),
+        _p(tt), _p(tg), _p(vz), int(nthreads),
+    )
+    if st == 1:
+        raise ValueError("source out of bound")
+    return tt, (tg if grad else None), vz
+
+
+def axes(shape, gridsize, origin):
+    return [origin[d] + gridsize[d] * np.arange(shape[d]) for d in range(len(shape))]
+
+
+def interp(ax, v, points, fill_value=np.nan, stride=1):
+    """Plain bi-/tri-linear interpolation (``_interp2d.py`` / ``_interp3d.py``).
+    ``v`` may be a strided gradient component: pass the full [..][stride] array
+    offset by the component via ``v[..., c]``'s base and ``stride``."""
+    pts = _c(np.atleast_2d(points))
+    out = np.empty(len(pts))
+    ax = [_c(a) for a in ax]
+    v = np.asarray(v)
+    if len(ax) == 3:
+        lib().oracle_interp3d(
+            _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(ax[2]), len(ax[2]),
+            ctypes.c_void_p(v.ctypes.data), stride, _p(pts), len(pts), float(fill_value), _p(out),
+        )
+    else:
+        lib().oracle_interp2d(
+            _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), ctypes.c_void_p(v.ctypes.data), stride,
+            _p(pts), len(pts), float(fill_value), _p(out),
+        )
+    return out
+
+
+def vinterp(ax, tt, points, source, vzero, fill_value=np.nan):
+    """Apparent-velocity traveltime interpolation (``_vinterp2d.py`` / ``_vinterp3d.py``)."""
+    pts = _c(np.atleast_2d(points))
+    out = np.empty(len(pts))
+    ax = [_c(a) for a in ax]
+    tt = _c(tt)
+    src = _c(source)
+    if len(ax) == 3:
+        lib().oracle_vinterp3d(
+            _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(ax[2]), len(ax[2]), _p(tt),
+            _p(pts), len(pts), _p(src), float(vzero), float(fill_value), _p(out),
+        )
+    else:
+        lib().oracle_vinterp2d(
+            _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(tt), _p(pts), len(pts), _p(src),
+            float(vzero), float(fill_value), _p(out),
+        )
+    return out
+
+
+def raytrace(ax, ttgrad, ends, source, stepsize, max_step, honor_grid=False):
+    """Ray tracing (``_ray2d.py`` / ``_ray3d.py``). Returns a list of rays, each
+    ordered source -> end point, as ``ray3d`` returns them."""
+    nd = len(ax)
+    ends = _c(np.atleast_2d(ends))
+    n = len(ends)
+    ax = [_c(a) for a in ax]
+    g = _c(ttgrad)
+    src = _c(source)
+    rays = np.zeros((n, int(max_step), nd))
+    counts = np.zeros(n, dtype=np.int32)
+    status = np.zeros(n, dtype=np.int32)
+    if nd == 3:
+        lib().oracle_ray3d(
+            _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(ax[2]), len(ax[2]), _p(g),
+            _p(ends), n, _p(src), float(stepsize), int(max_step), int(honor_grid), _p(rays),
+            _p(counts), _p(status),
+        )
+    else:
+        lib().oracle_ray2d(
+            _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(g), _p(ends), n, _p(src),
+            float(stepsize), int(max_step), int(honor_grid), _p(rays), _p(counts), _p(status),
+        )
+    if (status == 2).any():
+        raise ValueError("end point out of bound")
+    if (status == 3).any():
+        raise RuntimeError("maximum number of steps reached")
+    return [rays[r, counts[r]::-1].copy() for r in range(n)]

@@ -1,0 +1,26 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def golden3d():
+    import numpy as np
+
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "golden3d.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden2d():
+    import numpy as np
+
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "golden2d.npz")))

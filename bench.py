@@ -1,0 +1,461 @@
+"""Benchmark of the 3D traveltime path on GB300: the batched many-source solve.
+
+Workload (one step): a seeded layered float64 velocity model of 128 x 256 x 256
+cells at 10 m (6 layers with uniform velocities in [1500, 4500] m/s, interfaces
+perturbed by +-30 m of smoothed noise), 256 surface sources on a 16 x 16 grid
+with seeded off-grid jitter, nsweep=2 with gradients, all solved by one
+persistent kernel launch, then a-posteriori ray tracing from every source to
+400 seeded surface receivers (102,400 rays).
+
+Printed JSON line (rank 0):
+  value     shots/s with the model, sources and receivers resident in HBM
+  e2e       the same step through the drop-in Python API from host arrays
+            (velocity upload, solve, rays and first-arrival picks copied back)
+  plain     the same grid solved one source per launch (the "plain" solve)
+  roofline  the sweep kernel's FP64 rate against the FP64 peak measured in
+            this run, with its HBM rate beside it
+  cpu_baseline  the CPU oracle (C restatement of the reference, OpenMP over
+            all host cores) on a bounded sample of the same workload
+
+``--impl reference`` times the reference's CPU implementation instead: numba is
+not installed on these hosts, so this is the oracle's C restatement with all
+host threads (the reference's own pure-Python mode is ~1e4x slower still).
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D cell-updates/s & shots/s: batched vs plain GPU solve (FP64, rel err≤1e-12)"
+SHAPE = (128, 256, 256)
+D = (10.0, 10.0, 10.0)
+NSRC = 256
+NREC = 400
+NSWEEP = 2
+FLOP_PER_UPDATE = 160  # algorithmic FP64 operations of one 3D node update
+BYTES_PER_UPDATE = 25  # slowness + tt read + tt write (8 B each) + 1 B branch record
+
+
+def smooth2d(rng, shape, sigma):
+    from scipy.ndimage import gaussian_filter
+
+    p = gaussian_filter(rng.standard_normal(shape), sigma)
+    p -= p.min()
+    return 2.0 * p / p.max() - 1.0
+
+
+def layered_model(shape=SHAPE, d=D, nlayers=6, seed=2024):
+    """6 horizontal layers, seeded velocities in [1500, 4500] m/s, interfaces
+    perturbed by +-30 m of smoothed noise."""
+    rng = np.random.default_rng(seed)
+    nz, nx, ny = shape
+    depth = nz * d[0]
+    tops = np.sort(rng.uniform(0.1 * depth, 0.9 * depth, nlayers - 1))
+    vels = rng.uniform(1500.0, 4500.0, nlayers)
+    zc = (np.arange(nz) + 0.5) * d[0]
+    layer = np.zeros(shape, dtype=np.int64)
+    for t in tops:
+        iface = t + 30.0 * smooth2d(rng, (nx, ny), 8.0)
+        layer += zc[:, None, None] > iface[None, :, :]
+    return vels[layer]
+
+
+def surface_sources(shape=SHAPE, d=D, n_side=16, seed=7):
+    rng = np.random.default_rng(seed)
+    ext = np.array(shape) * np.array(d)
+    ix, iy = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
+    x = (ix.ravel() + 0.5 + rng.uniform(-0.3, 0.3, n_side**2)) * ext[1] / n_side
+    y = (iy.ravel() + 0.5 + rng.uniform(-0.3, 0.3, n_side**2)) * ext[2] / n_side
+    return np.column_stack([np.zeros(n_side**2), x, y])
+
+
+def surface_receivers(shape=SHAPE, d=D, n=NREC, seed=11):
+    rng = np.random.default_rng(seed)
+    ext = (np.array(shape) - 0) * np.array(d)  # node extent = cells * spacing
+    return np.column_stack(
+        [np.zeros(n), rng.uniform(0.0, ext[1], n), rng.uniform(0.0, ext[2], n)]
+    )
+
+
+def updates_per_source(shape=SHAPE, nsweep=NSWEEP):
+    return 8 * nsweep * int(np.prod(shape))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = (
+        "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": float(max(smax)) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(nthreads=None, nsrc=None, shape=SHAPE):
+    """Time the CPU oracle (all host cores, OpenMP over sources) on a bounded
+    sample of the workload: as many sources as threads, solved with gradients,
+    plus their rays. Returns (shots/s, threads, sample description)."""
+    from oracle import oracle as O
+
+    nthreads = nthreads or os.cpu_count() or 1
+    nsrc = nsrc or nthreads
+    v = layered_model(shape)
+    src = surface_sources(shape)[:nsrc]
+    rec = surface_receivers(shape)
+    O.lib()
+    t0 = time.perf_counter()
+    tt, tg, vz = O.solve3d(1.0 / v, D, src, NSWEEP, True, nthreads=nthreads)
+    ax = O.axes(tt.shape[1:], D, np.zeros(3))
+    max_dist = 2.0 * sum((n * h) ** 2 for n, h in zip(tt.shape[1:], D)) ** 0.5
+    for s in range(nsrc):
+        O.raytrace(ax, tg[s], rec, src[s], min(D), int(max_dist / min(D)), False)
+    dt = time.perf_counter() - t0
+    desc = (f"{nsrc} of the {NSRC} sources on the {shape[0]}x{shape[1]}x{shape[2]} grid "
+            f"(solve with gradients + {NREC} rays each), {nthreads} threads")
+    return nsrc / dt, nthreads, desc
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(nthreads)
+    times = []
+    for _ in range(args.steps):
+        sps, _, desc = cpu_sample(nthreads)
+        times.append(nthreads / sps)
+    ms = 1e3 * float(np.mean(times))
+    value = nthreads / (ms * 1e-3)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "shots/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded layered model, surface sources and receivers)",
+        "config": workload_config(),
+        "cell_updates_per_s": value * updates_per_source(),
+        "cpu_baseline": {
+            "value": value,
+            "unit": "shots/s",
+            "cores": nthreads,
+            "kind": "port",
+            "sample": desc + "; numba is not installed on this host, so the reference's "
+            "kernels run as the oracle's line-by-line C restatement (gcc -O2, OpenMP)",
+        },
+        "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config():
+    return {
+        "workload": "batched 3D solve: 256 surface sources on a 128x256x256 layered model "
+                    "(dz=dx=dy=10 m), nsweep=2 with gradients, then 256x400 rays",
+        "grid": list(SHAPE),
+        "sources": NSRC,
+        "receivers_per_source": NREC,
+        "nsweep": NSWEEP,
+        "cell_updates_per_source": updates_per_source(),
+        "l2": "inputs larger than L2 (17.4 GB of traveltimes per step)",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import fteikpy_gb300 as fp
+    from fteikpy_gb300 import _device, _lib, _solver
+    from fteikpy_gb300._grid import trace_rays_device
+
+    world, rank = dist_setup()
+    lib = _lib.load()
+    dev = _device.device()
+
+    v = layered_model()
+    src = surface_sources()
+    rec = surface_receivers()
+    nz, nx, ny = SHAPE
+    node_shape = (nz + 1, nx + 1, ny + 1)
+    axes = [_device.to_device(a) for a in
+            [np.arange(n) * h for n, h in zip(node_shape, D)]]
+    max_dist = 2.0 * sum((n * h) ** 2 for n, h in zip(node_shape, D)) ** 0.5
+    max_step = int(max_dist / min(D))
+
+    # resident inputs
+    slow = _device.slowness(_device.to_device(v))
+    ends = _device.to_device(np.tile(rec, (NSRC, 1)))
+    gidx = torch.arange(NSRC, dtype=torch.int32, device=dev).repeat_interleave(NREC)
+    src_dev = _device.to_device(src)
+    grad_stride = int(np.prod(node_shape)) * 3
+
+    lib.fteik_kernel_timing(1)
+    sweep_ms = []
+
+    def step():
+        tt, tg, vz = _solver.solve3d_device(slow, D, src, NSWEEP, True)
+        ms = __import__("ctypes").c_float()
+        lib.fteik_last_sweep_ms(ms)
+        sweep_ms.append(ms.value)
+        packed, lengths = trace_rays_device(3, axes, tg, gidx, ends, src_dev, min(D), max_step,
+                                            False, grad_stride)
+        return tt, tg, packed
+
+    for _ in range(args.warmup):
+        out = step()
+        del out
+    torch.cuda.synchronize()
+    sweep_ms.clear()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        out = step()
+        del out
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms_step = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    shots = NSRC * world / (ms_step * 1e-3)
+    sweep = float(np.mean(sweep_ms))
+
+    # roofline of the sweep kernel (one launch = all sweeps of all sources)
+    updates = updates_per_source() * NSRC
+    scratch = torch.empty(152 * 8 * 256, dtype=torch.float64, device=dev)
+    peak = __import__("ctypes").c_double()
+    lib.fteik_fp64_peak(_device.ptr(scratch), 152 * 8, 20000, peak, _device.stream())
+    achieved_tf = updates * FLOP_PER_UPDATE / (sweep * 1e-3) / 1e12
+    peak_tf = peak.value / 1e12
+    hbm_gbs = updates * BYTES_PER_UPDATE / (sweep * 1e-3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak = json.load(open(peaks_path))["hbm_gbs"] if os.path.exists(peaks_path) else 6800.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "sweep3d_traffic.json")
+    if os.path.exists(tpath):
+        t = json.load(open(tpath))
+        traffic = t["dram_bytes_per_update"] * updates
+
+    # plain: one source per launch on the same grid
+    plain_n = 4
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    for s in range(plain_n):
+        tt1, tg1, _ = _solver.solve3d_device(slow, D, src[s:s + 1], NSWEEP, True)
+        trace_rays_device(3, axes, tg1, None, _device.to_device(rec), src_dev[s:s + 1], min(D),
+                          max_step, False)
+        del tt1, tg1
+    torch.cuda.synchronize()
+    plain_ms = 1e3 * (time.perf_counter() - p0) / plain_n
+    plain_shots = 1e3 / plain_ms
+
+    # e2e through the drop-in API from host arrays
+    h2d = v.nbytes + src.nbytes + rec.nbytes * NSRC
+    d2h = [0]
+
+    def e2e_step():
+        eik = fp.Eikonal3D(v, D)
+        tts = eik.solve(src, nsweep=NSWEEP, return_gradient=True)
+        nb = 0
+        for t in tts:
+            rays = t.raytrace(rec)
+            picks = t(rec)
+            nb += sum(r.nbytes for r in rays) + picks.nbytes
+        d2h[0] = nb
+        return tts
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    q0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - q0) / args.e2e_steps, world)
+    e2e_shots = NSRC * world / (e2e_ms * 1e-3)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sps, cores, desc = cpu_sample()
+        cpu = {"value": sps, "unit": "shots/s", "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": shots,
+            "unit": "shots/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded layered model, surface sources and receivers)",
+            "config": workload_config(),
+            "cell_updates_per_s": shots * updates_per_source(),
+            "plain": {
+                "value": plain_shots,
+                "unit": "shots/s",
+                "ms_per_shot": plain_ms,
+                "what": "same grid, one source per solve launch (+ its 400 rays)",
+                "batched_over_plain": shots / world / plain_shots,
+            },
+            "roofline": {
+                "bound": "fp64",
+                "kernel": "sweep3d_kernel",
+                "achieved": achieved_tf,
+                "peak": peak_tf,
+                "unit": "TFLOP/s",
+                "frac": achieved_tf / peak_tf,
+                "flop_per_update": FLOP_PER_UPDATE,
+                "peak_source": "DFMA loop measured in this run (fteik_fp64_peak)",
+                "kernel_ms": sweep,
+                "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+                        "frac": hbm_gbs / hbm_peak, "bytes_per_update": BYTES_PER_UPDATE},
+                "traffic": traffic,
+            },
+            "e2e": {
+                "value": e2e_shots,
+                "unit": "shots/s",
+                "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h[0]),
+                "what": "Eikonal3D(host velocity).solve(256 sources, gradients) + "
+                        "raytrace and picks per source through the drop-in API",
+            },
+            "gpu_launches": 7 * args.steps,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

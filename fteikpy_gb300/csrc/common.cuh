@@ -1,0 +1,122 @@
+// Device helpers shared by the fteik_gb300 kernels (sm_103a, FP64).
+//
+// The kernels reproduce fteikpy's numba arithmetic operation by operation:
+// `x ** 2.0` is x*x, `x ** 0.5` is the correctly rounded sqrt, every other
+// operation is a single IEEE double operation in the reference's evaluation
+// order, and the library is compiled with --fmad=false so nothing is
+// contracted.  On GB300 the FP64 pipe is the bottleneck (about 1.2 TFLOP/s), so
+// work that can leave it without changing a single result bit does:
+//
+//  * comparisons, min and max of doubles run on the integer pipe through an
+//    order-preserving integer key of the bit pattern (exact for all non-NaN
+//    values; -0.0 never arises in these kernels);
+//  * multiplication by 0.5 or 4.0 (exact scalings) edits the exponent field;
+//  * division by a per-launch constant c uses a double-double reciprocal of c
+//    and one Markstein correction step, which returns the correctly rounded
+//    quotient (Markstein, "IA-64 and Elementary Functions", 2000, Thm. 8.?:
+//    a faithful quotient q plus r*y with r = a - b*q exact and y = RN(1/b)
+//    rounds to RN(a/b)); tests compare it against the IEEE division.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fteik {
+
+constexpr double kBig = 1.0e5;   // fteikpy/_fteik/_fteik3d.py:6, _fteik2d.py:6
+constexpr double kEps = 1.0e-15; // fteikpy/_fteik/_fteik3d.py:7, _fteik2d.py:7
+constexpr int kEpsin = 5;        // fteikpy/_fteik/_fteik2d.py:8
+
+// Status codes returned by every C-ABI entry point.
+enum Status : int {
+  kOk = 0,
+  kSourceOutOfBound = 1,
+  kEndPointOutOfBound = 2,
+  kMaxStepReached = 3,
+  kDeviceWaitTimeout = 4,
+  kInvalidArgument = 5,
+  kCudaError = 6,
+  kWorkspaceTooSmall = 7,
+};
+
+// ---- integer-pipe comparisons -------------------------------------------------
+
+// Order-preserving key: key(a) < key(b) <=> a < b for non-NaN doubles (with
+// -0.0 ordered before +0.0, which never arises here).
+__device__ __forceinline__ long long okey(double x) {
+  long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }
+__device__ __forceinline__ bool dle(double a, double b) { return okey(a) <= okey(b); }
+// Python min/max built-ins: keep the first argument unless strictly beaten.
+__device__ __forceinline__ double dmin(double a, double b) { return okey(b) < okey(a) ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return okey(b) > okey(a) ? b : a; }
+// Min of two positive doubles (slowness): the raw bit patterns order like the values.
+__device__ __forceinline__ double pmin(double a, double b) {
+  long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return __longlong_as_double(y < x ? y : x);
+}
+__device__ __forceinline__ bool deq(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// ---- exact power-of-two scalings ---------------------------------------------
+
+// 0.5 * x, exact for zero and for |x| >= 2^-1021 (the callers' precondition,
+// checked on the host from the model's scales).
+__device__ __forceinline__ double half(double x) {
+  long long b = __double_as_longlong(x);
+  return (b & 0x7ff0000000000000LL) ? __longlong_as_double(b - (1LL << 52)) : x;
+}
+// 4.0 * x, exact for zero and for normal x below 2^1021.
+__device__ __forceinline__ double times4(double x) {
+  long long b = __double_as_longlong(x);
+  return (b & 0x7ff0000000000000LL) ? __longlong_as_double(b + (2LL << 52)) : x;
+}
+
+// ---- correctly rounded division by a per-launch constant -----------------------
+
+struct Recip {
+  double c, hi, lo;  // c, RN(1/c), (1 - c*hi)/c
+};
+__host__ __device__ inline Recip make_recip(double c) {
+  Recip r;
+  r.c = c;
+  r.hi = 1.0 / c;
+#ifdef __CUDA_ARCH__
+  r.lo = __fma_rn(-c, r.hi, 1.0) / c;
+#else
+  r.lo = __builtin_fma(-c, r.hi, 1.0) / c;
+#endif
+  return r;
+}
+// RN(x / c) for finite x (no overflow/underflow), as IEEE division returns.
+__device__ __forceinline__ double div_by(double x, const Recip& r) {
+  double q = __fma_rn(x, r.hi, __dmul_rn(x, r.lo));  // faithful quotient
+  double rem = __fma_rn(-q, r.c, x);                 // exact remainder
+  return __fma_rn(rem, r.hi, q);                     // Markstein correction
+}
+
+// ---- misc ------------------------------------------------------------------------
+
+__device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
+__device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+
+// L2-coherent loads/stores for data exchanged between warps of a running kernel.
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+}  // namespace fteik

@@ -1,0 +1,471 @@
+// 2D FTeik solver for GB300: fteikpy/_fteik/_fteik2d.py rebuilt as CUDA.
+//
+// Layout (C order, float64 unless noted):
+//   slow  [nz][nx] cells, tt [nsrc][NZ][NX] nodes, ttgrad [nsrc][NZ][NX][2],
+//   rec   [nsrc][NZ][NX] uint8 branch record (sz+1)*3 + (sx+1) (ttsgn of
+//         _fteik2d.py:178-187).
+//
+// Schedule.  The reference's 2D sweep is NOT a set of independent directional
+// sweeps: for every column it runs the downward pass and then the upward pass
+// before moving to the next column (_fteik2d.py:199-287), so each sweep is a
+// single dependence chain of 4*nz*nx node updates, and reordering it changes
+// the result (by up to 1e-2 relative on layered models).  The kernel therefore
+// keeps the reference's order exactly: one thread walks one source's chain,
+// and batches of sources run in parallel, one thread each.
+#include <cstdint>
+
+#include "common.cuh"
+#include "fteik_gb300.h"
+#include "runtime.h"
+
+namespace fteik {
+
+struct Ops2 {
+  double dz, dx, dzi, dxi, dz2i, dx2i;  // sweep2d dargs, _fteik2d.py:193-197
+  double s2, p2;                        // dz2i + dx2i, dz2i * dx2i
+  double dzz, dxx, hyp;                 // dz**2, dx**2, (dx**2 + dz**2)**0.5
+  Recip r2, rdz, rdx, rhyp;
+};
+
+static Ops2 make_ops2(double dz, double dx) {
+  Ops2 o;
+  o.dz = dz;
+  o.dx = dx;
+  o.dzi = 1.0 / dz;
+  o.dxi = 1.0 / dx;
+  o.dz2i = o.dzi / dz;
+  o.dx2i = o.dxi / dx;
+  o.s2 = o.dz2i + o.dx2i;
+  o.p2 = o.dz2i * o.dx2i;
+  o.dzz = dz * dz;
+  o.dxx = dx * dx;
+  o.hyp = __builtin_sqrt(o.dxx + o.dzz);
+  o.r2 = make_recip(o.s2);
+  o.rdz = make_recip(dz);
+  o.rdx = make_recip(dx);
+  o.rhyp = make_recip(o.hyp);
+  return o;
+}
+
+struct Source2 {
+  double zsa, xsa, vzero;
+  int zsi, xsi, iflag, pad;
+};
+
+// t_ana / t_anad, _fteik2d.py:11-30.
+__device__ __forceinline__ double t_ana2(int i, int j, double dz, double dx, double zsa,
+                                         double xsa, double vzero) {
+  double a = dz * ((double)i - zsa);
+  double b = dx * ((double)j - xsa);
+  return vzero * sqrt(a * a + b * b);
+}
+__device__ __forceinline__ double t_anad2(int i, int j, double dz, double dx, double zsa,
+                                          double xsa, double vzero, double& tzc, double& txc) {
+  double t = t_ana2(i, j, dz, dx, zsa, xsa, vzero);
+  if (t > 0.0) {
+    double tmp = vzero * vzero / t;
+    tzc = ((double)i - zsa) * dz * tmp;
+    txc = ((double)j - xsa) * dx * tmp;
+  } else {
+    tzc = txc = 0.0;
+  }
+  return t;
+}
+
+// delta, _fteik2d.py:33-67 (factored quadratic near the source).
+__device__ double delta2(double t1, double tauv, double taue, double tauev, double t0c,
+                         double tzc, double txc, double dzi, double dxi, double dz2i,
+                         double dx2i, double vzero, double vref, int sgntz, int sgntx) {
+  double ta = tauev + taue - tauv;
+  double tb = tauev - taue + tauv;
+  double apoly = dz2i + dx2i;
+  double bpoly = 4.0 * ((double)sgntx * txc * dxi + (double)sgntz * tzc * dzi) -
+                 2.0 * (ta * dx2i + tb * dz2i);
+  double cpoly = ((ta * ta) * dx2i) + ((tb * tb) * dz2i) -
+                 4.0 * ((double)sgntx * txc * dxi * ta + (double)sgntz * tzc * dzi * tb) +
+                 4.0 * (vzero * vzero - vref * vref);
+  double dpoly = bpoly * bpoly - 4.0 * apoly * cpoly;
+  return dpoly >= 0.0 ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
+}
+
+// One node update, _fteik2d.py:70-187.  NZ, NX are node counts.  Comparisons
+// are IEEE comparisons here (not integer keys): after a source on the model's
+// far boundary the reference's first propagation can leave NaN in tt, and
+// Python's comparison and min semantics on NaN must be kept.
+template <bool GRAD>
+__device__ __forceinline__ void node_update2d(double* tt, uint8_t* rec, const double* slow,
+                                              const Ops2& o, const Source2& sp, int i, int j,
+                                              int sgnvz, int sgnvx, int sgntz, int sgntx,
+                                              int NZ, int NX) {
+  const int nxc = NX - 1;
+  const int i1 = i - sgnvz, j1 = j - sgnvx;
+  const long long n = (long long)i * NX + j;
+  const double tv = tt[n - (long long)sgntz * NX];
+  const double te = tt[n - sgntx];
+  const double tev = tt[n - (long long)sgntz * NX - sgntx];
+
+  double vref = pmin(slow[(long long)i1 * nxc + imax(j - 1, 0)], slow[(long long)i1 * nxc + imin(j, NX - 2)]);
+  const double t1d1 = tv + o.dz * vref;
+  vref = pmin(slow[(long long)imax(i - 1, 0) * nxc + j1], slow[(long long)imin(i, NZ - 2) * nxc + j1]);
+  const double t1d2 = te + o.dx * vref;
+  const double t1d = t1d2 < t1d1 ? t1d2 : t1d1;
+
+  double t2d = kBig;
+  vref = slow[(long long)i1 * nxc + j1];
+  const int di = i - sp.zsi, dj = j - sp.xsi;
+  if (di > kEpsin || di < -kEpsin || dj > kEpsin || dj < -kEpsin) {
+    // plane-wave operators, _fteik2d.py:121-142
+    if (tv <= te + o.dx * vref && te <= tv + o.dz * vref && te >= tev && tv >= tev) {
+      const double ta = tev + te - tv;
+      const double tb = tev - te + tv;
+      const double d = ta - tb;
+      t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(times4(vref * vref) * o.s2 - o.p2 * (d * d)),
+                   o.r2);
+    } else if (te - tev <= div_by(o.dzz * vref, o.rhyp) && te - tev > 0.0) {
+      const double q = div_by(te - tev, o.rdz);
+      t2d = te + o.dx * sqrt(vref * vref - q * q);
+    } else if (tv - tev <= div_by(o.dxx * vref, o.rhyp) && tv - tev > 0.0) {
+      const double q = div_by(tv - tev, o.rdx);
+      t2d = tv + o.dz * sqrt(vref * vref - q * q);
+    }
+  } else {
+    // spherical (factored) operator near the source, _fteik2d.py:144-171
+    if (tv < te + o.dx * vref && te < tv + o.dz * vref && te >= tev && tv >= tev) {
+      double tzc, txc;
+      const double t0c = t_anad2(i, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero, tzc, txc);
+      const double tauv = tv - t_ana2(i - sgntz, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
+      const double taue = te - t_ana2(i, j - sgntx, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
+      const double tauev = tev - t_ana2(i - sgntz, j - sgntx, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
+      t2d = delta2(t2d, tauv, taue, tauev, t0c, tzc, txc, o.dzi, o.dxi, o.dz2i, o.dx2i,
+                   sp.vzero, vref, sgntz, sgntx);
+      if (t2d < tv || t2d < te) t2d = kBig;
+    }
+  }
+  const double t0 = tt[n];
+  // min(t0, t1d, t2d) with Python's semantics: keep the earlier argument
+  // unless a later one compares strictly smaller.
+  double tnew = t0;
+  if (t1d < tnew) tnew = t1d;
+  if (t2d < tnew) tnew = t2d;
+  if (!(tnew == t0)) {
+    tt[n] = tnew;
+    if (GRAD) {
+      int a, b;
+      if (tnew == t1d1) {
+        a = sgntz; b = 0;
+      } else if (tnew == t1d2) {
+        a = 0; b = sgntx;
+      } else {
+        a = sgntz; b = sgntx;
+      }
+      rec[n] = (uint8_t)((a + 1) * 3 + (b + 1));
+    }
+  }
+}
+
+// Source classification and first propagation, _fteik2d.py:296-617, then the
+// nsweep interleaved sweeps, _fteik2d.py:190-287 and 619-621.  One thread per
+// source.  tt is pre-filled with Big and rec with "no sign".
+template <bool GRAD>
+__global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const double* src,
+                                                     int nsrc, int nz, int nx, int nsweep,
+                                                     Ops2 o, double* tt_all, uint8_t* rec_all,
+                                                     Source2* params, double* vzero_out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsrc) return;
+  const int NZ = nz + 1, NX = nx + 1;
+  const long long nodes = (long long)NZ * NX;
+  double* tt = tt_all + (long long)s * nodes;
+  uint8_t* rec = GRAD ? rec_all + (long long)s * nodes : nullptr;
+  const double dz = o.dz, dx = o.dx;
+#define TT(a, b) tt[(long long)(a)*NX + (b)]
+#define SL(a, b) slow[(long long)(a)*nx + (b)]
+#define SGN(a, b, sz_, sx_) \
+  if (GRAD) rec[(long long)(a)*NX + (b)] = (uint8_t)(((sz_) + 1) * 3 + ((sx_) + 1))
+
+  double zsa = src[2 * s] / dz, xsa = src[2 * s + 1] / dx;
+  zsa = zsa >= nz ? zsa - kEps : zsa;
+  xsa = xsa >= nx ? xsa - kEps : xsa;
+  const int zsi = imin((int)zsa, nz - 1);
+  const int xsi = imin((int)xsa, nx - 1);
+  const double vzero = SL(zsi, xsi);
+
+  double dzu = fabs(zsa - (double)zsi);
+  double dzd = 1.0 - dzu;
+  double dxw = fabs(xsa - (double)xsi);
+  double dxe = 1.0 - dxw;
+  const double dzv_min = dzd < dzu ? dzd : dzu;
+  const double dzh_min = dxe < dxw ? dxe : dxw;
+  int iflag;
+  if (dzv_min < kEps && dzh_min < kEps) {
+    zsa = rint(zsa);
+    xsa = rint(xsa);
+    iflag = 1;
+  } else if (dzv_min > kEps || dzh_min > kEps) {
+    zsa = dzv_min < kEps ? rint(zsa) : zsa;
+    xsa = dzh_min < kEps ? rint(xsa) : xsa;
+    iflag = 2;
+  } else {
+    zsa = rint(zsa);
+    xsa = rint(xsa);
+    iflag = 3;
+  }
+
+  if (iflag == 2) {
+    dzu = fabs(zsa - (double)zsi);
+    dzd = 1.0 - dzu;
+    dxw = fabs(xsa - (double)xsi);
+    dxe = 1.0 - dxw;
+    for (int q = 0; q < 4; ++q) {
+      const int i = zsi + (q & 1), j = xsi + (q >> 1);
+      double tzc, txc;
+      TT(i, j) = t_anad2(i, j, dz, dx, zsa, xsa, vzero, tzc, txc);
+    }
+    double dxi = 1.0 / dx;
+    double dx2i = dxi / dx;
+    double dzi, dz2i, tzc, txc, t0c, vref, tauv, tauev, taue, td_prev, td_cur;
+    // along row zsi (+1), eastwards, _fteik2d.py:379-435
+    td_prev = vzero * dxe * dx;
+    for (int j = xsi + 2; j < NX; ++j) {
+      vref = SL(zsi, j - 1);
+      td_cur = td_prev + dx * vref;
+      tauv = td_cur - vzero * fabs((double)j - xsa) * dx;
+      tauev = td_prev - vzero * fabs((double)j - xsa - 1.0) * dx;
+      dzi = 1.0 / dzd;
+      dz2i = dz / dzd / dzd;
+      taue = TT(zsi + 1, j - 1) - t_ana2(zsi + 1, j - 1, dz, dx, zsa, xsa, vzero);
+      t0c = t_anad2(zsi + 1, j, dz, dx, zsa, xsa, vzero, tzc, txc);
+      TT(zsi + 1, j) = delta2(TT(zsi + 1, j), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i,
+                              dx2i, vzero, vref, 1, 1);
+      SGN(zsi + 1, j, 1, 1);
+      if (dzu > 0.0) {
+        dzi = 1.0 / dzu;
+        dz2i = dz / dzu / dzu;
+        taue = TT(zsi, j - 1) - t_ana2(zsi, j - 1, dz, dx, zsa, xsa, vzero);
+        t0c = t_anad2(zsi, j, dz, dx, zsa, xsa, vzero, tzc, txc);
+        TT(zsi, j) = delta2(TT(zsi, j), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i, dx2i,
+                            vzero, vref, -1, 1);
+        SGN(zsi, j, -1, 1);
+      }
+      td_prev = td_cur;
+    }
+    // westwards, _fteik2d.py:437-495
+    td_prev = vzero * dxw * dx;
+    for (int j = xsi - 1; j >= 0; --j) {
+      vref = SL(zsi, j);
+      td_cur = td_prev + dx * vref;
+      tauv = td_cur - vzero * fabs((double)j - xsa) * dx;
+      tauev = td_prev - vzero * fabs((double)j - xsa + 1.0) * dx;
+      dzi = 1.0 / dzd;
+      dz2i = dz / dzd / dzd;
+      taue = TT(zsi + 1, j + 1) - t_ana2(zsi + 1, j + 1, dz, dx, zsa, xsa, vzero);
+      t0c = t_anad2(zsi + 1, j, dz, dx, zsa, xsa, vzero, tzc, txc);
+      TT(zsi + 1, j) = delta2(TT(zsi + 1, j), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i,
+                              dx2i, vzero, vref, 1, -1);
+      SGN(zsi + 1, j, 1, -1);
+      if (dzu > 0.0) {
+        dzi = 1.0 / dzu;
+        dz2i = dz / dzu / dzu;
+        // the reference reads row zsi + 1 here (_fteik2d.py:472-474)
+        taue = TT(zsi + 1, j + 1) - t_ana2(zsi + 1, j + 1, dz, dx, zsa, xsa, vzero);
+        t0c = t_anad2(zsi, j, dz, dx, zsa, xsa, vzero, tzc, txc);
+        TT(zsi, j) = delta2(TT(zsi, j), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i, dx2i,
+                            vzero, vref, -1, -1);
+        SGN(zsi, j, -1, -1);
+      }
+      td_prev = td_cur;
+    }
+    // along column xsi (+1), downwards, _fteik2d.py:497-556
+    dzi = 1.0 / dz;
+    dz2i = dzi / dz;
+    td_prev = vzero * dzd * dz;
+    for (int i = zsi + 2; i < NZ; ++i) {
+      vref = SL(i - 1, xsi);
+      td_cur = td_prev + dz * vref;
+      taue = td_cur - vzero * fabs((double)i - zsa) * dz;
+      tauev = td_prev - vzero * fabs((double)i - zsa - 1.0) * dz;
+      dxi = 1.0 / dxe;
+      dx2i = dx / dxe / dxe;
+      tauv = TT(i - 1, xsi + 1) - t_ana2(i - 1, xsi + 1, dz, dx, zsa, xsa, vzero);
+      t0c = t_anad2(i, xsi + 1, dz, dx, zsa, xsa, vzero, tzc, txc);
+      TT(i, xsi + 1) = delta2(TT(i, xsi + 1), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i,
+                              dx2i, vzero, vref, 1, 1);
+      SGN(i, xsi + 1, 1, 1);
+      if (dxw > 0.0) {
+        dxi = 1.0 / dxw;
+        dx2i = dx / dxw / dxw;
+        tauv = TT(i - 1, xsi) - t_ana2(i - 1, xsi, dz, dx, zsa, xsa, vzero);
+        t0c = t_anad2(i, xsi, dz, dx, zsa, xsa, vzero, tzc, txc);
+        TT(i, xsi) = delta2(TT(i, xsi), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i, dx2i,
+                            vzero, vref, 1, -1);
+        SGN(i, xsi, 1, -1);
+      }
+      td_prev = td_cur;
+    }
+    // upwards, _fteik2d.py:558-614
+    td_prev = vzero * dzu * dz;
+    for (int i = zsi - 1; i >= 0; --i) {
+      vref = SL(i, xsi);
+      td_cur = td_prev + dz * vref;
+      taue = td_cur - vzero * fabs((double)i - zsa) * dz;
+      tauev = td_prev - vzero * fabs((double)i - zsa + 1.0) * dz;
+      dxi = 1.0 / dxe;
+      dx2i = dx / dxe / dxe;
+      tauv = TT(i + 1, xsi + 1) - t_ana2(i + 1, xsi + 1, dz, dx, zsa, xsa, vzero);
+      t0c = t_anad2(i, xsi + 1, dz, dx, zsa, xsa, vzero, tzc, txc);
+      TT(i, xsi + 1) = delta2(TT(i, xsi + 1), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i,
+                              dx2i, vzero, vref, -1, 1);
+      SGN(i, xsi + 1, -1, 1);
+      if (dxw > 0.0) {
+        dxi = 1.0 / dxw;
+        dx2i = dx / dxw / dxw;
+        tauv = TT(i + 1, xsi) - t_ana2(i + 1, xsi, dz, dx, zsa, xsa, vzero);
+        t0c = t_anad2(i, xsi, dz, dx, zsa, xsa, vzero, tzc, txc);
+        TT(i, xsi) = delta2(TT(i, xsi), tauv, taue, tauev, t0c, tzc, txc, dzi, dxi, dz2i, dx2i,
+                            vzero, vref, -1, -1);
+        SGN(i, xsi, -1, -1);
+      }
+      td_prev = td_cur;
+    }
+  } else {
+    TT((int)zsa, (int)xsa) = 0.0;  // _fteik2d.py:616-617
+  }
+#undef TT
+#undef SL
+#undef SGN
+
+  Source2 sp;
+  sp.zsa = zsa;
+  sp.xsa = xsa;
+  sp.vzero = vzero;
+  sp.zsi = zsi;
+  sp.xsi = xsi;
+  sp.iflag = iflag;
+  sp.pad = 0;
+  params[s] = sp;
+  vzero_out[s] = vzero;
+
+  for (int sw = 0; sw < nsweep; ++sw) {
+    for (int j = 1; j < NX; ++j) {
+      for (int i = 1; i < NZ; ++i) node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 1, 1, 1, 1, NZ, NX);
+      for (int i = NZ - 2; i >= 0; --i)
+        node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 0, 1, -1, 1, NZ, NX);
+    }
+    for (int j = NX - 2; j >= 0; --j) {
+      for (int i = 1; i < NZ; ++i) node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 1, 0, 1, -1, NZ, NX);
+      for (int i = NZ - 2; i >= 0; --i)
+        node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 0, 0, -1, -1, NZ, NX);
+    }
+  }
+}
+
+__global__ void fill2d_kernel(double* tt, uint8_t* rec, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    tt[q] = kBig;
+    if (rec) rec[q] = 4;
+  }
+}
+
+// Gradient post-pass, _fteik2d.py:623-639.  With an off-grid source the 4
+// nodes around it start from their analytic derivatives (_fteik2d.py:370-375).
+__global__ void grad2d_kernel(const double* tt, const uint8_t* rec, const Source2* params,
+                              int nsrc, int NZ, int NX, double dz, double dx, double* ttgrad) {
+  const long long nodes = (long long)NZ * NX;
+  const long long total = nodes * nsrc;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(q / nodes);
+    const long long n = q - (long long)s * nodes;
+    const int i = (int)(n / NX), j = (int)(n - (long long)i * NX);
+    const Source2 p = params[s];
+    double g0 = 0.0, g1 = 0.0;
+    if (p.iflag == 2 && (unsigned)(i - p.zsi) <= 1u && (unsigned)(j - p.xsi) <= 1u)
+      t_anad2(i, j, dz, dx, p.zsa, p.xsa, p.vzero, g0, g1);
+    const int code = rec[q];
+    const int cz = code / 3 - 1, cx = code % 3 - 1;
+    const double tq = tt[q];
+    if (cz != 0) g0 = (double)cz * (tq - tt[q - (long long)cz * NX]) / dz;
+    if (cx != 0) g1 = (double)cx * (tq - tt[q - cx]) / dx;
+    const double gn = sqrt(g0 * g0 + g1 * g1);
+    if (gn > 0.0) {
+      g0 /= gn;
+      g1 /= gn;
+    }
+    ttgrad[2 * q] = g0;
+    ttgrad[2 * q + 1] = g1;
+  }
+}
+
+struct Layout2 {
+  size_t status, params, src, rec, total;
+};
+
+static size_t align_up2(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static Layout2 layout2(int nz, int nx, int nsrc, int grad) {
+  const size_t nodes = (size_t)(nz + 1) * (nx + 1);
+  Layout2 L;
+  size_t off = 0;
+  L.status = off;
+  off = align_up2(off + 16);
+  L.params = off;
+  off = align_up2(off + sizeof(Source2) * (size_t)nsrc);
+  L.src = off;
+  off = align_up2(off + sizeof(double) * 2 * (size_t)nsrc);
+  L.rec = off;
+  if (grad) off = align_up2(off + nodes * (size_t)nsrc);
+  L.total = off;
+  return L;
+}
+
+}  // namespace fteik
+
+using namespace fteik;
+
+extern "C" size_t fteik2d_workspace_bytes(int nz, int nx, int nsrc, int grad) {
+  if (nz < 1 || nx < 1 || nsrc < 1) return 0;
+  return layout2(nz, nx, nsrc, grad).total;
+}
+
+extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, double dx,
+                             const double* sources, int nsrc, int nsweep, int grad, double* tt,
+                             double* ttgrad, double* vzero, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nz < 2 || nx < 2 || nsrc < 1 || nsweep < 0 || !slow || !sources || !tt || !vzero ||
+      !workspace || (grad && !ttgrad))
+    return kInvalidArgument;
+  if (!(dz > 1e-100 && dz < 1e100 && dx > 1e-100 && dx < 1e100)) return kInvalidArgument;
+  const Layout2 L = layout2(nz, nx, nsrc, grad);
+  if (workspace_bytes < L.total) return kWorkspaceTooSmall;
+  for (int s = 0; s < nsrc; ++s) {  // _fteik2d.py:296-300
+    const double z = sources[2 * s], x = sources[2 * s + 1];
+    if (!((0.0 <= z && z <= dz * nz) && (0.0 <= x && x <= dx * nx))) return kSourceOutOfBound;
+  }
+  char* ws = (char*)workspace;
+  const Ops2 o = make_ops2(dz, dx);
+  Source2* params = (Source2*)(ws + L.params);
+  double* src_dev = (double*)(ws + L.src);
+  uint8_t* rec = grad ? (uint8_t*)(ws + L.rec) : nullptr;
+  const long long nodes = (long long)(nz + 1) * (nx + 1);
+  const long long ntot = nodes * nsrc;
+  FTEIK_CHECK(cudaMemsetAsync(ws + L.status, 0, 16, st));
+  FTEIK_CHECK(cudaMemcpyAsync(src_dev, sources, sizeof(double) * 2 * (size_t)nsrc,
+                              cudaMemcpyHostToDevice, st));
+  fill2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
+  const int blocks = (nsrc + 31) / 32;
+  if (grad)
+    solve2d_kernel<true><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt, rec,
+                                                 params, vzero);
+  else
+    solve2d_kernel<false><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt,
+                                                  rec, params, vzero);
+  FTEIK_CHECK(cudaGetLastError());
+  if (grad) {
+    grad2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, params, nsrc, nz + 1, nx + 1,
+                                                       dz, dx, ttgrad);
+    FTEIK_CHECK(cudaGetLastError());
+  }
+  return fteik_workspace_status(workspace, stream);
+}

@@ -1,0 +1,125 @@
+// Host-side runtime of the C ABI: error reporting, occupancy-derived launch
+// shapes, and the status word of a solve workspace.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+#include "common.cuh"
+#include "fteik_gb300.h"
+#include "runtime.h"
+
+namespace fteik {
+
+static thread_local char g_last_error[256] = "";
+
+int record_cuda_error(cudaError_t err, const char* what) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(err));
+  return kCudaError;
+}
+
+static int sm_count() {
+  static int count = 0;
+  if (count == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+    if (count <= 0) count = 1;
+  }
+  return count;
+}
+
+int resident_blocks(const void* kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(kernel);
+  if (it != cache.end()) return it->second;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int blocks = per_sm * sm_count();
+  cache[kernel] = blocks;
+  return blocks;
+}
+
+int grid_for(long long n, int threads) {
+  long long blocks = (n + threads - 1) / threads;
+  const long long cap = 8LL * sm_count();
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+static thread_local bool g_timing = false;
+static thread_local cudaEvent_t g_ev[2] = {nullptr, nullptr};
+
+void timing_events(cudaEvent_t* start, cudaEvent_t* stop) {
+  *start = g_timing ? g_ev[0] : nullptr;
+  *stop = g_timing ? g_ev[1] : nullptr;
+}
+
+// FP64 issue-rate probe: independent DFMA chains, 4 per thread.
+__global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3 + 1.0, x1 = x0 + 0.1, x2 = x0 + 0.2, x3 = x0 + 0.3;
+  for (int i = 0; i < iters; ++i) {
+    x0 = __fma_rn(x0, a, b);
+    x1 = __fma_rn(x1, a, b);
+    x2 = __fma_rn(x2, a, b);
+    x3 = __fma_rn(x3, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
+}
+
+}  // namespace fteik
+
+using namespace fteik;
+
+extern "C" int fteik_kernel_timing(int on) {
+  g_timing = on != 0;
+  if (g_timing && !g_ev[0]) {
+    FTEIK_CHECK(cudaEventCreate(&g_ev[0]));
+    FTEIK_CHECK(cudaEventCreate(&g_ev[1]));
+  }
+  return kOk;
+}
+
+extern "C" int fteik_last_sweep_ms(float* ms) {
+  if (!g_timing || !g_ev[1] || !ms) return kInvalidArgument;
+  FTEIK_CHECK(cudaEventSynchronize(g_ev[1]));
+  FTEIK_CHECK(cudaEventElapsedTime(ms, g_ev[0], g_ev[1]));
+  return kOk;
+}
+
+extern "C" int fteik_fp64_peak(double* scratch, int nblocks, int iters, double* flops_per_s,
+                               void* stream) {
+  if (!scratch || nblocks < 1 || iters < 1 || !flops_per_s) return kInvalidArgument;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  FTEIK_CHECK(cudaEventCreate(&e0));
+  FTEIK_CHECK(cudaEventCreate(&e1));
+  fp64_probe_kernel<<<nblocks, 256, 0, st>>>(scratch, 16, 0.999999, 1e-7);
+  FTEIK_CHECK(cudaEventRecord(e0, st));
+  fp64_probe_kernel<<<nblocks, 256, 0, st>>>(scratch, iters, 0.999999, 1e-7);
+  FTEIK_CHECK(cudaEventRecord(e1, st));
+  FTEIK_CHECK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  FTEIK_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *flops_per_s = 2.0 * 4.0 * iters * (double)nblocks * 256.0 / (ms * 1e-3);
+  return kOk;
+}
+
+extern "C" const char* fteik_version(void) { return "fteik_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" const char* fteik_last_error(void) { return g_last_error; }
+
+extern "C" int fteik_workspace_status(const void* workspace, void* stream) {
+  FTEIK_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+  int status = 0;
+  FTEIK_CHECK(cudaMemcpy(&status, workspace, sizeof(int), cudaMemcpyDeviceToHost));
+  return status;
+}

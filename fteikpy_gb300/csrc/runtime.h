@@ -1,0 +1,27 @@
+// Host-side helpers shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fteik {
+
+// Records the CUDA error text for fteik_last_error() and returns kCudaError.
+int record_cuda_error(cudaError_t err, const char* what);
+
+#define FTEIK_CHECK(call)                                          \
+  do {                                                             \
+    cudaError_t err_ = (call);                                     \
+    if (err_ != cudaSuccess) return record_cuda_error(err_, #call); \
+  } while (0)
+
+// Blocks of `threads` threads that stay resident at once on the current
+// device for `kernel` (cached per kernel).
+int resident_blocks(const void* kernel, int threads, size_t smem = 0);
+
+// Grid size for a grid-stride loop over n items: a multiple of the SM count.
+int grid_for(long long n, int threads);
+
+// When kernel timing is on (fteik_kernel_timing), the pair of events that the
+// 3D solve records around its sweep kernel on the launching stream; else null.
+void timing_events(cudaEvent_t* start, cudaEvent_t* stop);
+
+}  // namespace fteik

@@ -1,0 +1,162 @@
+/*
+ * fteik_gb300 C ABI: the drop-in boundary of fteikpy's traveltime path.
+ *
+ * Every entry point takes plain pointers and sizes. Arrays named "device" live
+ * in GPU memory owned by the caller; the library never allocates memory for
+ * results or scratch (the caller passes a workspace of the size the matching
+ * *_workspace_bytes function returns). `stream` is a cudaStream_t (NULL = the
+ * legacy default stream). Arrays use the reference's C-order layouts:
+ * cells [nz][nx](ny), nodes [nz+1][nx+1](ny+1), gradients [nodes][ndim],
+ * batched arrays with a leading source axis.
+ *
+ * Return value: 0 on success, else one of FTEIK_* below. The blocking calls
+ * synchronise `stream` before returning so that device-side failures (a ray
+ * hitting max_step, a dependency wait that timed out) are reported.
+ */
+#ifndef FTEIK_GB300_H
+#define FTEIK_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FTEIK_OK 0
+#define FTEIK_SOURCE_OUT_OF_BOUND 1   /* ValueError("source out of bound") */
+#define FTEIK_END_POINT_OUT_OF_BOUND 2 /* ValueError("end point out of bound") */
+#define FTEIK_MAX_STEP_REACHED 3      /* RuntimeError("maximum number of steps reached") */
+#define FTEIK_DEVICE_WAIT_TIMEOUT 4   /* a bounded device-side wait gave up */
+#define FTEIK_INVALID_ARGUMENT 5
+#define FTEIK_CUDA_ERROR 6
+#define FTEIK_WORKSPACE_TOO_SMALL 7
+
+/* Library version and a short description of the last CUDA error, if any. */
+const char* fteik_version(void);
+const char* fteik_last_error(void);
+
+/* Measurement hooks (no counterpart in the reference, which has no timing).
+ * fteik_kernel_timing(1) makes the 3D solve record CUDA events around its
+ * sweep kernel on the launching stream; fteik_last_sweep_ms then returns that
+ * kernel's duration. fteik_fp64_peak times a DFMA loop (nblocks x 256 threads,
+ * 4 chains each; `scratch` holds nblocks*256 doubles) and returns FLOP/s. */
+int fteik_kernel_timing(int on);
+int fteik_last_sweep_ms(float* ms);
+int fteik_fp64_peak(double* scratch, int nblocks, int iters, double* flops_per_s, void* stream);
+
+/* ---------------------------------------------------------- model set-up --
+ * slowness = 1.0 / velocity, as Eikonal2D/3D.solve does before calling the
+ * solver (fteikpy/_solver.py:49-50,120-121), for n values on the device.
+ * `flag` is a device int used as scratch. Blocking; returns
+ * FTEIK_INVALID_ARGUMENT when a slowness is not finite or lies outside
+ * (1e-150, 1e150) (the solver kernels need its square to be a normal double). */
+int fteik_slowness(const double* velocity, long long n, double* slow, int* flag, void* stream);
+
+/* ---------------------------------------------------------------- 3D solve --
+ * Replaces solve3d / fteik3d / fteik3d_vectorized
+ * (fteikpy/_fteik/_fteik3d.py:394-525) as called by Eikonal3D.solve
+ * (fteikpy/_solver.py:120-126).
+ *
+ *  slow      device [nz][nx][ny] slowness (1 / velocity), cell counts nz, nx, ny
+ *  sources   HOST   [nsrc][3] source (z, x, y) relative to the grid origin
+ *  tt        device [nsrc][nz+1][nx+1][ny+1] traveltimes (output)
+ *  ttgrad    device [nsrc][nz+1][nx+1][ny+1][3] unit gradients (output; may be
+ *            NULL when grad == 0)
+ *  vzero     device [nsrc] slowness at each source cell (output)
+ *  workspace device scratch of at least fteik3d_workspace_bytes(...) bytes
+ *  spin_limit maximum polls of one dependency wait before the kernel gives up
+ *            with FTEIK_DEVICE_WAIT_TIMEOUT (<= 0: default)
+ * All sources are solved by one persistent kernel launch that runs every
+ * directional sweep of every source.
+ */
+size_t fteik3d_workspace_bytes(int nz, int nx, int ny, int nsrc, int grad);
+int fteik3d_solve(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,
+                  const double* sources, int nsrc, int nsweep, int grad, double* tt,
+                  double* ttgrad, double* vzero, void* workspace, size_t workspace_bytes,
+                  long long spin_limit, void* stream);
+/* Same work, enqueued on `stream` without waiting; the status is read later
+ * with fteik_workspace_status(). Host-side argument errors return at once. */
+int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                        double dy, const double* sources, int nsrc, int nsweep, int grad,
+                        double* tt, double* ttgrad, double* vzero, void* workspace,
+                        size_t workspace_bytes, long long spin_limit, void* stream);
+/* Synchronise `stream` and return the device-side status of the last solve
+ * enqueued with this workspace. */
+int fteik_workspace_status(const void* workspace, void* stream);
+
+/* ---------------------------------------------------------------- 2D solve --
+ * Replaces solve2d / fteik2d / fteik2d_vectorized
+ * (fteikpy/_fteik/_fteik2d.py:290-674) as called by Eikonal2D.solve
+ * (fteikpy/_solver.py:49-55). Same conventions as the 3D solve with
+ * sources HOST [nsrc][2], tt [nsrc][nz+1][nx+1], ttgrad [...][2]. */
+size_t fteik2d_workspace_bytes(int nz, int nx, int nsrc, int grad);
+int fteik2d_solve(const double* slow, int nz, int nx, double dz, double dx,
+                  const double* sources, int nsrc, int nsweep, int grad, double* tt,
+                  double* ttgrad, double* vzero, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
+/* ---------------------------------------------------------- interpolation --
+ * interp3d / interp2d (fteikpy/_interp/_interp3d.py:188-195,
+ * _interp2d.py:88-95): bi-/tri-linear interpolation of v at query points, as
+ * used by Grid*.__call__ (fteikpy/_base.py:56-79,139-163) and by the gradient
+ * grids of TraveltimeGrid*.gradient (fteikpy/_grid.py:147-158,267-278).
+ *  ax0..ax2  device node axes (ascending), lengths n0..n2
+ *  v         device values [n0][n1](n2), element i read at v[i * vstride]
+ *  points    device [npts][ndim]
+ *  out       device [npts]; fill_value where a point lies outside the axes. */
+int fteik_interp3d(const double* ax0, int n0, const double* ax1, int n1, const double* ax2,
+                   int n2, const double* v, long long vstride, const double* points, int npts,
+                   double fill_value, double* out, void* stream);
+int fteik_interp2d(const double* ax0, int n0, const double* ax1, int n1, const double* v,
+                   long long vstride, const double* points, int npts, double fill_value,
+                   double* out, void* stream);
+
+/* vinterp3d / vinterp2d (fteikpy/_interp/_vinterp3d.py:280-291,
+ * _vinterp2d.py:122-131): apparent-velocity traveltime interpolation, as used
+ * by TraveltimeGrid*.__call__ (fteikpy/_grid.py:76-101,193-219). Batched: query
+ * point p is read from traveltime grid tt + grid_index[p] * tt_stride with
+ * source sources[grid_index[p]] and vzero[grid_index[p]]; grid_index may be
+ * NULL (all points use grid 0).
+ *  sources   device [ngrids][ndim] absolute source coordinates
+ *  vzero     device [ngrids] */
+int fteik_vinterp3d(const double* ax0, int n0, const double* ax1, int n1, const double* ax2,
+                    int n2, const double* tt, long long tt_stride, const int* grid_index,
+                    const double* points, int npts, const double* sources, const double* vzero,
+                    double fill_value, double* out, void* stream);
+int fteik_vinterp2d(const double* ax0, int n0, const double* ax1, int n1, const double* tt,
+                    long long tt_stride, const int* grid_index, const double* points, int npts,
+                    const double* sources, const double* vzero, double fill_value, double* out,
+                    void* stream);
+
+/* ------------------------------------------------------------ ray tracing --
+ * ray3d / ray2d (fteikpy/_fteik/_ray3d.py:167-208, _ray2d.py:120-153) as
+ * called by TraveltimeGrid*.raytrace (fteikpy/_grid.py:103-145,221-265).
+ * Batched: ray r starts at end point ends[r] and walks down the gradient grid
+ * ttgrad + grid_index[r] * grad_stride towards sources[grid_index[r]]
+ * (grid_index may be NULL: all rays use grid 0).
+ *  ttgrad    device [..][nodes][ndim] unit gradient grids
+ *  ends      device [nrays][ndim] end points (receivers)
+ *  rays      device [nrays][max_step][ndim] scratch output: ray r written end
+ *            point first; rays[r][counts[r]] is the source
+ *  counts    device [nrays] index of the last point of each ray
+ *  status    device [nrays] per-ray FTEIK_* code
+ * fteik_ray*_pack then writes the rays source-first (the order ray3d returns)
+ * and back to back into packed[sum(counts + 1)][ndim], ray r starting at row
+ * offsets[r] (device, exclusive prefix sum of counts + 1). */
+int fteik_ray3d(const double* ax0, int n0, const double* ax1, int n1, const double* ax2, int n2,
+                const double* ttgrad, long long grad_stride, const int* grid_index,
+                const double* ends, int nrays, const double* sources, double stepsize,
+                int max_step, int honor_grid, double* rays, int* counts, int* status,
+                void* stream);
+int fteik_ray2d(const double* ax0, int n0, const double* ax1, int n1, const double* ttgrad,
+                long long grad_stride, const int* grid_index, const double* ends, int nrays,
+                const double* sources, double stepsize, int max_step, int honor_grid,
+                double* rays, int* counts, int* status, void* stream);
+int fteik_ray_pack(int ndim, const double* rays, int nrays, int max_step, const int* counts,
+                   const long long* offsets, double* packed, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FTEIK_GB300_H */

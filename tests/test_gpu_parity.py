@@ -1,0 +1,314 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's own outputs.
+
+Tolerances: the kernels reproduce the reference's IEEE operation sequence
+without contraction, so traveltimes, gradients, interpolated values and ray
+coordinates are compared bit for bit against the C oracle, which follows the
+same semantics. Against the golden fixtures produced by the pure-Python
+reference (which evaluates ``x ** 0.5`` / ``x ** 2.0`` through ``pow``) the
+bound is the contract's 1e-12 relative.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import fteikpy_gb300 as fp
+from fteikpy_gb300 import _device, _solver
+from helpers import (
+    REF_CORNERS_2D,
+    REF_CORNERS_3D,
+    REF_GRAD_2D,
+    REF_GRAD_2D_SRC35,
+    REF_GRAD_3D,
+    REF_MESHIO_2D,
+    REF_MESHIO_3D,
+    REF_RAY_2D,
+    REF_RAY_3D,
+    REF_SOLVE_2D,
+    REF_SOLVE_3D,
+    REF_TT_2D,
+    REF_TT_3D,
+    default_max_step,
+    max_rel,
+    model_axes,
+)
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # the contract: max relative error against the reference
+
+
+def layered3d(shape, seed, d=(10.0, 10.0, 10.0)):
+    rng = np.random.default_rng(seed)
+    nz = shape[0]
+    tops = np.sort(rng.integers(1, nz, 3))
+    vels = np.sort(rng.uniform(1500.0, 4500.0, 4))
+    v = vels[np.searchsorted(tops, np.arange(nz), side="right")][:, None, None] * np.ones(shape)
+    v *= 1.0 + 0.05 * rng.uniform(-1.0, 1.0, shape)
+    return v
+
+
+def rand_sources(rng, shape, d, n, origin):
+    ext = np.array(shape) * np.array(d)
+    return origin + rng.uniform(0.0, 1.0, (n, len(shape))) * ext
+
+
+def bitwise(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.int64), b.view(np.int64))
+
+
+# ---------------------------------------------------------------- known answers
+
+
+@pytest.mark.parametrize("src", list(REF_SOLVE_3D))
+def test_known_answer_solve3d(src):
+    eik = fp.Eikonal3D(np.ones((16, 16, 16)), (1.0, 1.0, 1.0))
+    tt = eik.solve(list(src), nsweep=3)
+    assert np.allclose(tt.grid.sum(), REF_SOLVE_3D[src], atol=1e-8)
+    tts = eik.solve([list(s) for s in REF_SOLVE_3D], nsweep=3)
+    assert np.allclose([t.grid.sum() for t in tts], list(REF_SOLVE_3D.values()), atol=1e-8)
+
+
+@pytest.mark.parametrize("src", list(REF_SOLVE_2D))
+def test_known_answer_solve2d(src):
+    eik = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
+    tt = eik.solve(list(src), nsweep=2)
+    assert np.allclose(tt.grid.sum(), REF_SOLVE_2D[src], atol=1e-8)
+    tts = eik.solve([list(s) for s in REF_SOLVE_2D], nsweep=2)
+    assert np.allclose([t.grid.sum() for t in tts], list(REF_SOLVE_2D.values()), atol=1e-8)
+
+
+def test_known_answer_call_gradient_raytrace_3d():
+    eik = fp.Eikonal3D(np.ones((16, 16, 16)), (1.0, 1.0, 1.0))
+    assert eik([0.0, 0.0, 0.0]) == 1.0
+    assert np.isnan(eik([-1.0, -1.0, -1.0]))
+    assert np.allclose(eik(REF_CORNERS_3D), np.ones(8))
+    tt = eik.solve([0.0, 0.0, 0.0], nsweep=3, return_gradient=True)
+    for p, ref in REF_TT_3D:
+        got = tt(p)
+        assert (np.isnan(got) and np.isnan(ref)) or np.allclose(got, ref, atol=1e-8)
+    for c in range(3):
+        assert np.allclose(tt.gradient[c](REF_CORNERS_3D), REF_GRAD_3D[c], atol=1e-8)
+        assert np.isnan(tt.gradient[c]([-1.0, -1.0, -1.0]))
+    for end, hg, s in REF_RAY_3D:
+        assert np.allclose(tt.raytrace(end, stepsize=1.0, honor_grid=hg).sum(), s, atol=1e-8)
+    for hg in (False, True):
+        ends = [e for e, h, _ in REF_RAY_3D if h == hg]
+        sums = [s for _, h, s in REF_RAY_3D if h == hg]
+        rays = tt.raytrace(ends, stepsize=1.0, honor_grid=hg)
+        assert np.allclose([r.sum() for r in rays], sums, atol=1e-8)
+
+
+def test_known_answer_call_gradient_raytrace_2d():
+    eik = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
+    assert eik([0.0, 0.0]) == 1.0
+    assert np.allclose(eik(REF_CORNERS_2D), np.ones(4))
+    tt = eik.solve([0.0, 0.0], nsweep=2, return_gradient=True)
+    for p, ref in REF_TT_2D:
+        got = tt(p)
+        assert (np.isnan(got) and np.isnan(ref)) or np.allclose(got, ref, atol=1e-8)
+    for c in range(2):
+        assert np.allclose(tt.gradient[c](REF_CORNERS_2D), REF_GRAD_2D[c], atol=1e-8)
+    for end, hg, s in REF_RAY_2D:
+        assert np.allclose(tt.raytrace(end, stepsize=1.0, honor_grid=hg).sum(), s, atol=1e-8)
+    tt = eik.solve([3.5, 3.5], nsweep=2, return_gradient=True)
+    assert np.allclose([tt.gradient[c]([0.0, 0.0]) for c in range(2)], REF_GRAD_2D_SRC35, atol=1e-8)
+
+
+@pytest.mark.parametrize("case", [REF_MESHIO_2D, REF_MESHIO_3D])
+def test_known_answer_meshio_sums(case):
+    nd = len(case["shape"])
+    cls = fp.Eikonal3D if nd == 3 else fp.Eikonal2D
+    eik = cls(np.ones(case["shape"]), (1.0,) * nd)
+    tt = eik.solve(case["source"], return_gradient=True)
+    assert np.allclose(tt.grid.sum(), case["tt_sum"], atol=1e-8)
+    ray = tt.raytrace(np.zeros(nd), honor_grid=True)
+    assert len(ray) == case["ray_len"]
+
+
+# ------------------------------------------------------------- golden fixtures
+
+
+@pytest.mark.parametrize("nd", [2, 3])
+def test_golden_solve_and_interp(nd, golden2d, golden3d):
+    g = golden3d if nd == 3 else golden2d
+    cls = fp.Eikonal3D if nd == 3 else fp.Eikonal2D
+    eik = cls(g["velocity"], g["gridsize"], g["origin"])
+    tts = eik.solve(g["sources"], nsweep=int(g["nsweep"]), return_gradient=True)
+    tt = np.stack([t.grid for t in tts])
+    assert max_rel(tt, g["tt"]) <= TOL
+    grad = np.stack([t._gradient.cpu().numpy() for t in tts])
+    assert np.abs(grad - g["ttgrad"]).max() <= 1e-10
+    assert np.array_equal([t._vzero for t in tts], g["vzero"])
+    for s, t in enumerate(tts):
+        assert max_rel(t(g["points"]), g["vinterp"][s]) <= TOL
+        for c in range(nd):
+            gi = t.gradient[c](g["points"])
+            assert np.array_equal(np.isnan(gi), np.isnan(g["gradinterp"][s][c]))
+            assert np.nanmax(np.abs(gi - g["gradinterp"][s][c])) <= 1e-10
+        for hg in (0, 1):
+            rays = t.raytrace(g["receivers"], honor_grid=bool(hg))
+            assert np.array_equal([len(r) for r in rays], g[f"raylen_s{s}_hg{hg}"])
+            assert np.abs(np.concatenate(rays) - g[f"rays_s{s}_hg{hg}"]).max() <= 1e-9
+    assert max_rel(eik(g["points"]), g["velinterp"]) == 0.0
+    if nd == 3:
+        t1 = eik.solve(g["sources"][0], nsweep=1, return_gradient=True)
+        assert max_rel(t1.grid, g["tt_nsweep1"]) <= TOL
+        rays = tts[0].raytrace(g["receivers"], stepsize=4.0)
+        assert np.array_equal([len(r) for r in rays], g["raylen_s0_step4"])
+    else:
+        t3 = eik.solve(g["sources"][:2], nsweep=3, return_gradient=True)
+        assert max_rel(np.stack([t.grid for t in t3]), g["tt_nsweep3"]) <= TOL
+        rays = tts[0].raytrace(g["receivers"], stepsize=3.0)
+        assert np.array_equal([len(r) for r in rays], g["raylen_s0_step3"])
+
+
+# ------------------------------------------------- bitwise against the oracle
+
+
+@pytest.mark.parametrize(
+    "shape,d,nsrc,nsweep,seed",
+    [
+        ((12, 14, 16), (9.0, 11.0, 10.0), 3, 2, 0),
+        ((2, 2, 2), (1.0, 1.0, 1.0), 2, 2, 1),
+        ((3, 17, 5), (4.0, 1.5, 2.5), 4, 3, 2),
+        ((40, 33, 47), (10.0, 10.0, 10.0), 5, 2, 3),
+        ((25, 9, 70), (7.0, 13.0, 5.0), 2, 1, 4),
+        ((30, 40, 24), (10.0, 10.0, 10.0), 1, 0, 5),
+    ],
+)
+def test_solve3d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed):
+    rng = np.random.default_rng(seed)
+    v = layered3d(shape, seed)
+    src = rand_sources(rng, shape, d, nsrc, np.zeros(3))
+    src[0, 0] = 0.0  # a surface source
+    if nsrc > 1:
+        src[1] = np.floor(src[1] / d) * d  # on a node
+    tt_o, tg_o, vz_o = O.solve3d(1.0 / v, d, src, nsweep, True)
+    eik = fp.Eikonal3D(v, d)
+    tts = eik.solve(src, nsweep=nsweep, return_gradient=True)
+    tt = np.stack([t.grid for t in tts])
+    tg = np.stack([t._gradient.cpu().numpy() for t in tts])
+    assert max_rel(tt, tt_o) <= TOL
+    assert bitwise(tt, tt_o), f"{(tt != tt_o).sum()} of {tt.size} traveltimes differ in bits"
+    assert bitwise(tg, tg_o), f"{(tg != tg_o).sum()} gradient components differ in bits"
+    assert np.array_equal([t._vzero for t in tts], vz_o)
+    # without gradients the traveltimes are the same
+    tt_ng = np.stack([t.grid for t in eik.solve(src, nsweep=nsweep)])
+    assert bitwise(tt_ng, tt_o)
+
+
+@pytest.mark.parametrize("nsrc", [1, 7, 64])
+def test_solve3d_batched_equals_single(nsrc):
+    rng = np.random.default_rng(100 + nsrc)
+    shape, d = (20, 26, 30), (10.0, 10.0, 10.0)
+    v = layered3d(shape, 7)
+    src = rand_sources(rng, shape, d, nsrc, np.zeros(3))
+    eik = fp.Eikonal3D(v, d)
+    batch = eik.solve(src, nsweep=2, return_gradient=True)
+    for i in sorted({0, nsrc // 2, nsrc - 1}):
+        one = eik.solve(src[i], nsweep=2, return_gradient=True)
+        assert bitwise(one.grid, batch[i].grid)
+        assert bitwise(one._gradient.cpu().numpy(), batch[i]._gradient.cpu().numpy())
+    tt_o, _, _ = O.solve3d(1.0 / v, d, src[[0, nsrc - 1]], 2, False)
+    assert bitwise(batch[0].grid, tt_o[0]) and bitwise(batch[-1].grid, tt_o[1])
+
+
+@pytest.mark.parametrize(
+    "shape,d,nsrc,nsweep,seed",
+    [
+        ((24, 32), (10.0, 8.0), 5, 2, 0),
+        ((2, 2), (1.0, 1.0), 2, 2, 1),
+        ((60, 45), (5.0, 7.0), 9, 3, 2),
+        ((13, 90), (10.0, 10.0), 3, 1, 3),
+    ],
+)
+def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed):
+    rng = np.random.default_rng(seed)
+    v = 1500.0 + 30.0 * np.arange(shape[0])[:, None] * np.ones(shape)
+    v *= 1.0 + 0.1 * rng.uniform(-1.0, 1.0, shape)
+    src = rand_sources(rng, shape, d, nsrc, np.zeros(2))
+    src[0, 0] = 0.0
+    if nsrc > 1:
+        src[1] = np.floor(src[1] / d) * d
+    tt_o, tg_o, vz_o = O.solve2d(1.0 / v, d, src, nsweep, True)
+    tts = fp.Eikonal2D(v, d).solve(src, nsweep=nsweep, return_gradient=True)
+    tt = np.stack([t.grid for t in tts])
+    tg = np.stack([t._gradient.cpu().numpy() for t in tts])
+    assert max_rel(tt, tt_o) <= TOL
+    assert bitwise(tt, tt_o), f"{(tt != tt_o).sum()} of {tt.size} traveltimes differ in bits"
+    assert bitwise(tg, tg_o)
+
+
+def test_interp_and_rays_bitwise_vs_oracle():
+    rng = np.random.default_rng(9)
+    shape, d, og = (20, 24, 28), (10.0, 12.0, 8.0), np.array([3.0, -5.0, 7.0])
+    v = layered3d(shape, 9)
+    src = og + np.array([0.0, 131.7, 97.3])
+    eik = fp.Eikonal3D(v, d, og)
+    tt = eik.solve(src, nsweep=2, return_gradient=True)
+    tg = tt._gradient.cpu().numpy()
+    ax = model_axes(tt.shape, d, og)
+    hi = og + np.array(d) * (np.array(tt.shape) - 1)
+    pts = rng.uniform(og - 3.0, hi + 3.0, (2000, 3))
+    assert bitwise(tt(pts), O.vinterp(ax, tt.grid, pts, src, tt._vzero))
+    for c in range(3):
+        assert bitwise(tt.gradient[c](pts), O.interp(ax, tg[..., c], pts, stride=3))
+    rec = np.column_stack([np.full(300, og[0]), rng.uniform(og[1], hi[1], 300), rng.uniform(og[2], hi[2], 300)])
+    for hg in (False, True):
+        stepsize = min(d)
+        ms = default_max_step(tt.shape, d, stepsize)
+        # Some honor_grid rays walk along cell faces until max_step in the
+        # reference as well: both sides must fail on exactly those rays.
+        fails = []
+        for i in range(len(rec)):
+            try:
+                O.raytrace(ax, tg, rec[i : i + 1], src, stepsize, ms, hg)
+            except RuntimeError:
+                fails.append(i)
+        for i in fails:
+            with pytest.raises(RuntimeError, match="maximum number of steps reached"):
+                tt.raytrace(rec[i], honor_grid=hg)
+        keep = np.setdiff1d(np.arange(len(rec)), fails)
+        got = tt.raytrace(rec[keep], honor_grid=hg)
+        ref = O.raytrace(ax, tg, rec[keep], src, stepsize, ms, hg)
+        assert [len(r) for r in got] == [len(r) for r in ref]
+        assert bitwise(np.concatenate(got), np.concatenate(ref))
+
+
+def test_errors_match_reference():
+    eik = fp.Eikonal3D(np.ones((6, 6, 6)), (1.0, 1.0, 1.0))
+    with pytest.raises(ValueError, match="source out of bound"):
+        eik.solve([7.0, 0.0, 0.0])
+    tt = eik.solve([0.0, 0.0, 0.0], return_gradient=True)
+    with pytest.raises(ValueError, match="end point out of bound"):
+        tt.raytrace([[1.0, 1.0, 1.0], [7.0, 0.0, 0.0]])
+    with pytest.raises(RuntimeError, match="maximum number of steps reached"):
+        tt.raytrace([6.0, 6.0, 6.0], stepsize=0.1, max_step=5)
+    with pytest.raises(ValueError, match="no gradient grid"):
+        eik.solve([0.0, 0.0, 0.0]).gradient
+
+
+def test_device_wait_timeout_is_reported_and_recoverable():
+    """A dependency wait that runs out reports an error status, the kernel
+    returns, and the context stays usable (no GPU fault, no hang)."""
+    v = layered3d((30, 40, 48), 11)
+    slow = _device.slowness(_device.to_device(v))
+    src = np.array([[0.0, 150.0, 200.0]])
+    with pytest.raises(RuntimeError, match="timed out"):
+        _solver.solve3d_device(slow, (10.0, 10.0, 10.0), src, 2, True, spin_limit=1)
+    tt, _, _ = _solver.solve3d_device(slow, (10.0, 10.0, 10.0), src, 2, True)
+    tt_o, _, _ = O.solve3d(1.0 / v, (10.0, 10.0, 10.0), src, 2, False)
+    assert bitwise(tt.cpu().numpy(), tt_o)
+
+
+def test_torch_cuda_grid_is_used_in_place():
+    v = layered3d((10, 12, 14), 12)
+    vt = torch.as_tensor(v, device="cuda")
+    a = fp.Eikonal3D(vt, (10.0, 10.0, 10.0)).solve([0.0, 30.0, 40.0])
+    b = fp.Eikonal3D(v, (10.0, 10.0, 10.0)).solve([0.0, 30.0, 40.0])
+    assert bitwise(a.grid, b.grid)

@@ -1,0 +1,143 @@
+"""CPU-only checks of the CUDA library and the host-side logic (no GPU needed).
+
+The library is built here (nvcc cross-compiles sm_103a), loaded with ctypes,
+and must export every entry point that include/fteik_gb300.h declares. The
+host-side validation of the C ABI (argument checks, source bounds, workspace
+sizes) runs before any CUDA call, so it is exercised here through the C ABI
+with placeholder pointers that are never dereferenced.
+"""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import fteikpy_gb300 as fp
+from fteikpy_gb300 import _build, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fteik_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fteik[0-9a-z_]*)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "fteik3d_solve" in names and "fteik2d_solve" in names
+    assert len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+    assert b"sm_103a" in lib.fteik_version()
+
+
+def test_workspace_sizes(lib):
+    small = lib.fteik3d_workspace_bytes(4, 5, 6, 1, 0)
+    with_grad = lib.fteik3d_workspace_bytes(4, 5, 6, 1, 1)
+    assert with_grad >= small + 5 * 6 * 7  # one branch-record byte per node
+    assert lib.fteik3d_workspace_bytes(4, 5, 6, 8, 1) > with_grad
+    assert lib.fteik3d_workspace_bytes(0, 5, 6, 1, 1) == 0
+    assert lib.fteik2d_workspace_bytes(10, 12, 3, 1) >= 3 * 11 * 13
+    for b in (small, with_grad, lib.fteik2d_workspace_bytes(10, 12, 3, 1)):
+        assert b % 256 == 0
+
+
+FAKE = ctypes.c_void_p(0x1000)  # never dereferenced: the calls fail host-side first
+
+
+def _solve3d(lib, src, nz=4, nx=5, ny=6, d=(1.0, 1.0, 1.0), ws_bytes=None, nsweep=2):
+    src = np.ascontiguousarray(np.atleast_2d(src), dtype=np.float64)
+    ws = ws_bytes if ws_bytes is not None else lib.fteik3d_workspace_bytes(nz, nx, ny, len(src), 1)
+    return lib.fteik3d_solve(
+        FAKE, nz, nx, ny, *d, src.ctypes.data_as(ctypes.c_void_p), len(src), nsweep, 1, FAKE,
+        FAKE, FAKE, FAKE, ws, 0, None,
+    )
+
+
+def test_source_out_of_bound_is_host_side(lib):
+    # fteikpy/_fteik/_fteik3d.py:403-407: 0 <= src <= d * n on every axis
+    assert _solve3d(lib, [4.0 + 1e-9, 0.0, 0.0]) == _lib.SOURCE_OUT_OF_BOUND
+    assert _solve3d(lib, [0.0, -1e-12, 0.0]) == _lib.SOURCE_OUT_OF_BOUND
+    assert _solve3d(lib, [[1.0, 1.0, 1.0], [0.0, 0.0, 6.5]]) == _lib.SOURCE_OUT_OF_BOUND
+    assert _solve3d(lib, [np.nan, 0.0, 0.0]) == _lib.SOURCE_OUT_OF_BOUND
+    src = np.ascontiguousarray([[0.0, 5.5, 0.0]])
+    rc = lib.fteik2d_solve(FAKE, 4, 5, 1.0, 1.0, src.ctypes.data_as(ctypes.c_void_p), 1, 2, 1,
+                           FAKE, FAKE, FAKE, FAKE, lib.fteik2d_workspace_bytes(4, 5, 1, 1), None)
+    assert rc == _lib.SOURCE_OUT_OF_BOUND
+
+
+def test_invalid_arguments_are_host_side(lib):
+    assert _solve3d(lib, [0.0, 0.0, 0.0], ws_bytes=16) == _lib.WORKSPACE_TOO_SMALL
+    assert _solve3d(lib, [0.0, 0.0, 0.0], nz=1) == _lib.INVALID_ARGUMENT
+    assert _solve3d(lib, [0.0, 0.0, 0.0], d=(0.0, 1.0, 1.0)) == _lib.INVALID_ARGUMENT
+    assert _solve3d(lib, [0.0, 0.0, 0.0], nsweep=-1) == _lib.INVALID_ARGUMENT
+    rc = lib.fteik3d_solve(None, 4, 5, 6, 1.0, 1.0, 1.0, None, 1, 2, 0, None, None, None, None,
+                           0, 0, None)
+    assert rc == _lib.INVALID_ARGUMENT
+    assert lib.fteik_ray_pack(4, FAKE, 1, 10, FAKE, FAKE, FAKE, None) == _lib.INVALID_ARGUMENT
+    assert lib.fteik_ray3d(FAKE, 3, FAKE, 3, FAKE, 3, FAKE, 0, None, FAKE, 1, FAKE, 1.0, 1, 0,
+                           FAKE, FAKE, FAKE, None) == _lib.INVALID_ARGUMENT
+
+
+def test_status_codes_map_to_reference_exceptions():
+    with pytest.raises(ValueError, match="source out of bound"):
+        _lib.check(_lib.SOURCE_OUT_OF_BOUND)
+    with pytest.raises(ValueError, match="end point out of bound"):
+        _lib.check(_lib.END_POINT_OUT_OF_BOUND)
+    with pytest.raises(RuntimeError, match="maximum number of steps reached"):
+        _lib.check(_lib.MAX_STEP_REACHED)
+    with pytest.raises(RuntimeError, match="timed out"):
+        _lib.check(_lib.DEVICE_WAIT_TIMEOUT)
+    _lib.check(_lib.OK)
+
+
+def test_api_host_logic():
+    # fteikpy tests/test_misc.py:4-7
+    fp.set_num_threads(1)
+    assert fp.get_num_threads() == 1
+    v = np.full((4, 5, 6), 2.0)
+    eik = fp.Eikonal3D(v, (1.0, 2.0, 3.0), origin=(1.0, 0.0, -1.0))
+    assert eik.shape == (4, 5, 6) and eik.ndim == 3 and eik.size == 120
+    assert eik.gridsize == (1.0, 2.0, 3.0)
+    assert np.array_equal(eik.zaxis, 1.0 + np.arange(4))
+    assert np.array_equal(eik.yaxis, -1.0 + 3.0 * np.arange(6))
+    assert eik[0, 0, 0] == 2.0
+    tt = fp.TraveltimeGrid3D(np.zeros((5, 6, 7)), (1.0, 1.0, 1.0), np.zeros(3), [0, 0, 0], None, 1.0)
+    with pytest.raises(ValueError, match="no gradient grid"):
+        tt.gradient
+    with pytest.raises(ValueError, match="no gradient grid"):
+        tt.raytrace([1.0, 1.0, 1.0])
+    tt2 = fp.TraveltimeGrid2D(np.zeros((5, 6)), (1.0, 1.0), np.zeros(2), [0, 0], None, 1.0)
+    with pytest.raises(ValueError, match="no gradient grid"):
+        tt2.gradient
+
+
+def test_resample_and_smooth_match_reference_semantics():
+    # fteikpy tests/test_eikonal3d.py:48-60 and test_eikonal2d.py:36-48
+    eik = fp.Eikonal3D(np.ones((16, 16, 16)), (1.0, 1.0, 1.0))
+    eik.resample((32, 32, 32))
+    assert eik.grid.sum() == 16 * 16 * 16 * 8.0
+    eik = fp.Eikonal3D(np.ones((16, 16, 16)), (1.0, 1.0, 1.0))
+    eik.smooth(1.0)
+    assert eik.grid.sum() == eik.grid.size
+    eik2 = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
+    eik2.resample((32, 32))
+    assert eik2.grid.sum() == 16 * 16 * 4.0
+    eik2 = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
+    eik2.smooth(1.0)
+    assert eik2.grid.sum() == eik2.grid.size

@@ -53,9 +53,10 @@ def smooth2d(rng, shape, sigma):
     return 2.0 * p / p.max() - 1.0
 
 
-def layered_model(shape=SHAPE, d=D, nlayers=6, seed=2024):
+def layered_model(shape=None, d=D, nlayers=6, seed=2024):
     """6 horizontal layers, seeded velocities in [1500, 4500] m/s, interfaces
     perturbed by +-30 m of smoothed noise."""
+    shape = shape or SHAPE
     rng = np.random.default_rng(seed)
     nz, nx, ny = shape
     depth = nz * d[0]
@@ -69,7 +70,8 @@ def layered_model(shape=SHAPE, d=D, nlayers=6, seed=2024):
     return vels[layer]
 
 
-def surface_sources(shape=SHAPE, d=D, n_side=16, seed=7):
+def surface_sources(shape=None, d=D, n_side=16, seed=7):
+    shape = shape or SHAPE
     rng = np.random.default_rng(seed)
     ext = np.array(shape) * np.array(d)
     ix, iy = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
@@ -78,7 +80,8 @@ def surface_sources(shape=SHAPE, d=D, n_side=16, seed=7):
     return np.column_stack([np.zeros(n_side**2), x, y])
 
 
-def surface_receivers(shape=SHAPE, d=D, n=NREC, seed=11):
+def surface_receivers(shape=None, d=D, n=NREC, seed=11):
+    shape = shape or SHAPE
     rng = np.random.default_rng(seed)
     ext = (np.array(shape) - 0) * np.array(d)  # node extent = cells * spacing
     return np.column_stack(
@@ -86,7 +89,8 @@ def surface_receivers(shape=SHAPE, d=D, n=NREC, seed=11):
     )
 
 
-def updates_per_source(shape=SHAPE, nsweep=NSWEEP):
+def updates_per_source(shape=None, nsweep=NSWEEP):
+    shape = shape or SHAPE
     return 8 * nsweep * int(np.prod(shape))
 
 
@@ -185,12 +189,13 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-def cpu_sample(nthreads=None, nsrc=None, shape=SHAPE):
+def cpu_sample(nthreads=None, nsrc=None, shape=None):
     """Time the CPU oracle (all host cores, OpenMP over sources) on a bounded
     sample of the workload: as many sources as threads, solved with gradients,
     plus their rays. Returns (shots/s, threads, sample description)."""
     from oracle import oracle as O
 
+    shape = shape or SHAPE
     nthreads = nthreads or os.cpu_count() or 1
     nsrc = nsrc or nthreads
     v = layered_model(shape)
@@ -255,14 +260,16 @@ def run_reference(args):
 
 def workload_config():
     return {
-        "workload": "batched 3D solve: 256 surface sources on a 128x256x256 layered model "
-                    "(dz=dx=dy=10 m), nsweep=2 with gradients, then 256x400 rays",
+        "workload": f"batched 3D solve: {NSRC} surface sources on a "
+                    f"{SHAPE[0]}x{SHAPE[1]}x{SHAPE[2]} layered model "
+                    f"(dz=dx=dy=10 m), nsweep=2 with gradients, then {NSRC}x{NREC} rays",
         "grid": list(SHAPE),
         "sources": NSRC,
         "receivers_per_source": NREC,
         "nsweep": NSWEEP,
         "cell_updates_per_source": updates_per_source(),
-        "l2": "inputs larger than L2 (17.4 GB of traveltimes per step)",
+        "l2": "inputs larger than L2 (%.1f GB of traveltimes per step)"
+              % (NSRC * np.prod(np.array(SHAPE) + 1) * 8 / 1e9),
     }
 
 
@@ -274,7 +281,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end API timing")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-source-per-launch timing")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: 8 sources on a 64x128x128 grid (inputs still > L2)")
     args = ap.parse_args()
+    if args.small:
+        global SHAPE, NSRC
+        SHAPE, NSRC = (64, 128, 128), 8
     if args.impl == "reference":
         return run_reference(args)
 
@@ -289,7 +303,7 @@ def main():
     dev = _device.device()
 
     v = layered_model()
-    src = surface_sources()
+    src = surface_sources()[:NSRC]
     rec = surface_receivers()
     nz, nx, ny = SHAPE
     node_shape = (nz + 1, nx + 1, ny + 1)
@@ -357,7 +371,7 @@ def main():
         traffic = t["dram_bytes_per_update"] * updates
 
     # plain: one source per launch on the same grid
-    plain_n = 4
+    plain_n = 0 if args.no_plain else 4
     torch.cuda.synchronize()
     p0 = time.perf_counter()
     for s in range(plain_n):
@@ -366,8 +380,8 @@ def main():
                           max_step, False)
         del tt1, tg1
     torch.cuda.synchronize()
-    plain_ms = 1e3 * (time.perf_counter() - p0) / plain_n
-    plain_shots = 1e3 / plain_ms
+    plain_ms = 1e3 * (time.perf_counter() - p0) / max(plain_n, 1)
+    plain_shots = 1e3 / plain_ms if plain_n else None
 
     # e2e through the drop-in API from host arrays
     h2d = v.nbytes + src.nbytes + rec.nbytes * NSRC
@@ -384,16 +398,18 @@ def main():
         d2h[0] = nb
         return tts
 
-    e2e_step()
-    torch.cuda.synchronize()
-    barrier(world)
-    q0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    e2e_shots = None
+    if not args.no_e2e and args.e2e_steps > 0:
         e2e_step()
-    torch.cuda.synchronize()
-    barrier(world)
-    e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - q0) / args.e2e_steps, world)
-    e2e_shots = NSRC * world / (e2e_ms * 1e-3)
+        torch.cuda.synchronize()
+        barrier(world)
+        q0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - q0) / args.e2e_steps, world)
+        e2e_shots = NSRC * world / (e2e_ms * 1e-3)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -421,7 +437,7 @@ def main():
                 "unit": "shots/s",
                 "ms_per_shot": plain_ms,
                 "what": "same grid, one source per solve launch (+ its 400 rays)",
-                "batched_over_plain": shots / world / plain_shots,
+                "batched_over_plain": (shots / world / plain_shots) if plain_shots else None,
             },
             "roofline": {
                 "bound": "fp64",

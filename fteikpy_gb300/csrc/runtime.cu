@@ -1,5 +1,6 @@
 // Host-side runtime of the C ABI: error reporting, occupancy-derived launch
 // shapes, and the status word of a solve workspace.
+#include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -16,6 +17,13 @@ static thread_local char g_last_error[256] = "";
 int record_cuda_error(cudaError_t err, const char* what) {
   std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(err));
   return kCudaError;
+}
+
+void set_last_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
 }
 
 static int sm_count() {

@@ -7,6 +7,9 @@ namespace fteik {
 // Records the CUDA error text for fteik_last_error() and returns kCudaError.
 int record_cuda_error(cudaError_t err, const char* what);
 
+// Records a formatted message for fteik_last_error().
+void set_last_error(const char* fmt, ...);
+
 #define FTEIK_CHECK(call)                                          \
   do {                                                             \
     cudaError_t err_ = (call);                                     \

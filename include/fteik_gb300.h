@@ -84,6 +84,25 @@ int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, double dz, d
  * enqueued with this workspace. */
 int fteik_workspace_status(const void* workspace, void* stream);
 
+/* 3D solve that allocates nothing. No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc or hand over a device workspace (a
+ * framework that owns all device memory, a latency-critical loop where an
+ * allocation would synchronise the device, a foreign-language binding that can
+ * only pass the buffers it already owns). Same arguments and results as
+ * fteik3d_solve without the workspace: the scratch is a fixed array of
+ * FTEIK_NOALLOC_SCRATCH_BYTES compiled into the library, which every GPU that
+ * loads the library keeps until exit. Problems whose fteik3d_workspace_bytes()
+ * exceed it are rejected with FTEIK_WORKSPACE_TOO_SMALL. All calls on a device
+ * share the array (it keeps the last call's contents; the solve clears what
+ * must start at zero), so calls that overlap on the GPU race: serialise them.
+ * The first call on each device does a one-time set-up with that device
+ * current; make it before any stream capture. Blocking. */
+#define FTEIK_NOALLOC_SCRATCH_BYTES (64u << 20)
+int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                          double dy, const double* sources, int nsrc, int nsweep, int grad,
+                          double* tt, double* ttgrad, double* vzero, long long spin_limit,
+                          void* stream);
+
 /* ---------------------------------------------------------------- 2D solve --
  * Replaces solve2d / fteik2d / fteik2d_vectorized
  * (fteikpy/_fteik/_fteik2d.py:290-674) as called by Eikonal2D.solve

@@ -24,6 +24,7 @@ SIGNATURES = {
     "fteik_last_error": (ctypes.c_char_p, []),
     "fteik_slowness": (_I, [_P, _LL, _P, _P, _P]),
     "fteik_kernel_timing": (_I, [_I]),
+    "fteik_set_option": (_I, [ctypes.c_char_p, _LL]),
     "fteik_last_sweep_ms": (_I, [ctypes.POINTER(ctypes.c_float)]),
     "fteik_fp64_peak": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double), _P]),
     "fteik3d_workspace_bytes": (_SZ, [_I, _I, _I, _I, _I]),

@@ -39,11 +39,14 @@ constexpr int kPJ = 4;  // pencil width along x (j)
 constexpr int kPK = 8;  // pencil width along y (k)
 constexpr int kLag = kPJ + kPK - 2;
 constexpr int kWarpsPerBlock = 4;
+// Batches of at least this many sources read precomputed coefficient arrays.
+constexpr int kCoefMinSources = 4;
 
 struct Ops3 {
   double dz, dx, dy, dz2i, dx2i, dy2i, dz2dx2, dz2dy2, dx2dy2, dsum;
   double szx, szy, sxy;  // dz2i + dx2i, dz2i + dy2i, dx2i + dy2i
   Recip rzx, rzy, rxy, rsum;
+  Recip rdz, rdx, rdy;  // for the gradient post-pass
 };
 
 // Per-sweep constants, _fteik3d.py:208-215.
@@ -66,6 +69,9 @@ static Ops3 make_ops3(double dz, double dx, double dy) {
   o.rzy = make_recip(o.szy);
   o.rxy = make_recip(o.sxy);
   o.rsum = make_recip(o.dsum);
+  o.rdz = make_recip(dz);
+  o.rdx = make_recip(dx);
+  o.rdy = make_recip(dy);
   return o;
 }
 
@@ -96,67 +102,124 @@ __device__ __forceinline__ double t_anad3(int i, int j, int k, const Ops3& o, co
 }
 
 // Plane operator of _fteik3d.py:113-117 (and its ZY / XY twins):
-//   ((p*cp + q*cq) + sqrt(4*v^2*sum - prod*(ta-tb)^2)) / sum
+//   ((p*cp + q*cq) + sqrt(q4 - prod*(ta-tb)^2)) / sum,  q4 = 4*v^2*sum
 __device__ __forceinline__ double plane_op(double p, double cp, double q, double cq, double d,
-                                           double v, double sum, double prod, const Recip& r) {
+                                           double q4, double prod, const Recip& r) {
   double num = p * cp + q * cq;
-  double rad = times4(v * v) * sum - prod * (d * d);
+  double rad = q4 - prod * (d * d);
   return div_by(num + sqrt(rad), r);
 }
 
-// One node update, _fteik3d.py:38-200.  U[a][b][c] are the 8 slowness cells
-// around the node, indexed upwind-first: a = 0 is the reference's cell row i1
-// (i - sgnvz), a = 1 the other row of the pair {max(i-1,0), min(i,nz-2)};
-// b, c likewise along j, k.  Every min of the reference runs over a set of
-// these cells (the order inside a min does not change its value).
-template <bool GRAD>
+// Slowness-only operator coefficients, the same for every source and sweep,
+// computed once per solve by coef3d_kernel.  Node-shaped arrays with node
+// strides; the index in brackets is where the update reads them, with
+// (i1, j1, k1) the reference's upwind cell (i - sgnvz, ...):
+//   z1[i1][j][k]   = dz * min of the 4 cells of row i1 around column (j, k)
+//   x1[i][j1][k], y1[i][j][k1]: the same along x and y      (_fteik3d.py:76-102)
+//   zx?[i1][j1][k] from v = min(s[i1,j1,max(k-1,0)], s[i1,j1,min(k,ny-2)]):
+//        a = dx*v, b = dz*v, q = 4*v^2*(dz2i+dx2i)           (_fteik3d.py:109-117)
+//   zy?[i1][j][k1], xy?[i][j1][k1]: the ZY and XY planes     (_fteik3d.py:121-141)
+//   t3[i1][j1][k1] = s^2 * dsum * 9                          (_fteik3d.py:148,153)
+struct Coef3 {
+  double *z1, *x1, *y1, *zxa, *zxb, *zxq, *zya, *zyb, *zyq, *xya, *xyb, *xyq, *t3;
+};
+constexpr int kNumCoef = 13;
+
+// Where the update gets its coefficients from.  Both give the same values:
+//  * CoefArrays reads the precomputed arrays (one read each; pays off when
+//    many sources share them, as they then stay in L2);
+//  * CoefCells derives them from the 8 slowness cells around the node,
+//    U[a][b][c] indexed upwind-first (a = 0 is the reference's cell row i1 =
+//    i - sgnvz, a = 1 the other row of the pair {max(i-1,0), min(i,nz-2)};
+//    b, c likewise along j, k), which stay in L2 for any number of sources.
+struct CoefArrays {
+  const Coef3& C;
+  long long oz1, ox1, oy1, ozx, ozy, oxy, ot3;
+  __device__ __forceinline__ double z1() const { return __ldg(C.z1 + oz1); }
+  __device__ __forceinline__ double x1() const { return __ldg(C.x1 + ox1); }
+  __device__ __forceinline__ double y1() const { return __ldg(C.y1 + oy1); }
+  __device__ __forceinline__ double zxa() const { return __ldg(C.zxa + ozx); }
+  __device__ __forceinline__ double zxb() const { return __ldg(C.zxb + ozx); }
+  __device__ __forceinline__ double zxq() const { return __ldg(C.zxq + ozx); }
+  __device__ __forceinline__ double zya() const { return __ldg(C.zya + ozy); }
+  __device__ __forceinline__ double zyb() const { return __ldg(C.zyb + ozy); }
+  __device__ __forceinline__ double zyq() const { return __ldg(C.zyq + ozy); }
+  __device__ __forceinline__ double xya() const { return __ldg(C.xya + oxy); }
+  __device__ __forceinline__ double xyb() const { return __ldg(C.xyb + oxy); }
+  __device__ __forceinline__ double xyq() const { return __ldg(C.xyq + oxy); }
+  __device__ __forceinline__ double t3() const { return __ldg(C.t3 + ot3); }
+};
+
+struct CoefCells {
+  double U[2][2][2];
+  const Ops3& o;
+  __device__ __forceinline__ double vzx() const { return pmin(U[0][0][0], U[0][0][1]); }
+  __device__ __forceinline__ double vzy() const { return pmin(U[0][0][0], U[0][1][0]); }
+  __device__ __forceinline__ double vxy() const { return pmin(U[0][0][0], U[1][0][0]); }
+  __device__ __forceinline__ double z1() const {
+    return o.dz * pmin(pmin(U[0][0][0], U[0][0][1]), pmin(U[0][1][0], U[0][1][1]));
+  }
+  __device__ __forceinline__ double x1() const {
+    return o.dx * pmin(pmin(U[0][0][0], U[1][0][0]), pmin(U[0][0][1], U[1][0][1]));
+  }
+  __device__ __forceinline__ double y1() const {
+    return o.dy * pmin(pmin(U[0][0][0], U[0][1][0]), pmin(U[1][0][0], U[1][1][0]));
+  }
+  __device__ __forceinline__ double zxa() const { return o.dx * vzx(); }
+  __device__ __forceinline__ double zxb() const { return o.dz * vzx(); }
+  __device__ __forceinline__ double zxq() const { const double v = vzx(); return times4(v * v) * o.szx; }
+  __device__ __forceinline__ double zya() const { return o.dy * vzy(); }
+  __device__ __forceinline__ double zyb() const { return o.dz * vzy(); }
+  __device__ __forceinline__ double zyq() const { const double v = vzy(); return times4(v * v) * o.szy; }
+  __device__ __forceinline__ double xya() const { return o.dy * vxy(); }
+  __device__ __forceinline__ double xyb() const { return o.dx * vxy(); }
+  __device__ __forceinline__ double xyq() const { const double v = vxy(); return times4(v * v) * o.sxy; }
+  __device__ __forceinline__ double t3() const { return U[0][0][0] * U[0][0][0] * o.dsum * 9.0; }
+};
+
+// One node update, _fteik3d.py:38-200, with the slowness-only factors taken
+// from the coefficient provider c (see Coef3 for which factor is which).
+template <bool GRAD, class CP>
 __device__ __forceinline__ double node_update3d(double tv, double te, double tn, double tev,
                                                 double ten, double tnv, double tnve, double t0,
-                                                const double (&U)[2][2][2], const Ops3& o,
-                                                int sz, int sx, int sy, uint8_t& code) {
+                                                const CP& c, const Ops3& o, int sz, int sx,
+                                                int sy, uint8_t& code) {
   // 1D operators, _fteik3d.py:76-104
-  double v = pmin(pmin(U[0][0][0], U[0][0][1]), pmin(U[0][1][0], U[0][1][1]));
-  const double t1d1 = tv + o.dz * v;
-  v = pmin(pmin(U[0][0][0], U[1][0][0]), pmin(U[0][0][1], U[1][0][1]));
-  const double t1d2 = te + o.dx * v;
-  v = pmin(pmin(U[0][0][0], U[0][1][0]), pmin(U[1][0][0], U[1][1][0]));
-  const double t1d3 = tn + o.dy * v;
+  const double t1d1 = tv + c.z1();
+  const double t1d2 = te + c.x1();
+  const double t1d3 = tn + c.y1();
   const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
 
   // 2D operators, _fteik3d.py:106-143
   double t2d1 = kBig;
-  v = pmin(U[0][0][0], U[0][0][1]);
-  if (dlt(tv, te + o.dx * v) && dlt(te, tv + o.dz * v)) {
+  if (dlt(tv, te + c.zxa()) && dlt(te, tv + c.zxb())) {
     double ta = tev + te - tv;
     double tb = tev - te + tv;
-    t2d1 = plane_op(tb, o.dz2i, ta, o.dx2i, ta - tb, v, o.szx, o.dz2dx2, o.rzx);
+    t2d1 = plane_op(tb, o.dz2i, ta, o.dx2i, ta - tb, c.zxq(), o.dz2dx2, o.rzx);
   }
   double t2d2 = kBig;
-  v = pmin(U[0][0][0], U[0][1][0]);
-  if (dlt(tv, tn + o.dy * v) && dlt(tn, tv + o.dz * v)) {
+  if (dlt(tv, tn + c.zya()) && dlt(tn, tv + c.zyb())) {
     double ta = tv - tn + tnv;
     double tb = tn - tv + tnv;
-    t2d2 = plane_op(ta, o.dz2i, tb, o.dy2i, ta - tb, v, o.szy, o.dz2dy2, o.rzy);
+    t2d2 = plane_op(ta, o.dz2i, tb, o.dy2i, ta - tb, c.zyq(), o.dz2dy2, o.rzy);
   }
   double t2d3 = kBig;
-  v = pmin(U[0][0][0], U[1][0][0]);
-  if (dlt(te, tn + o.dy * v) && dlt(tn, te + o.dx * v)) {
+  if (dlt(te, tn + c.xya()) && dlt(tn, te + c.xyb())) {
     double ta = te - tn + ten;
     double tb = tn - te + ten;
-    t2d3 = plane_op(ta, o.dx2i, tb, o.dy2i, ta - tb, v, o.sxy, o.dx2dy2, o.rxy);
+    t2d3 = plane_op(ta, o.dx2i, tb, o.dy2i, ta - tb, c.xyq(), o.dx2dy2, o.rxy);
   }
   const double t2d = dmin(dmin(t2d1, t2d2), t2d3);
 
   // 3D operator, _fteik3d.py:145-159
   double t3d = kBig;
   if (dlt(dmax(dmax(tv, te), tn), dmin(t1d, t2d))) {
-    v = U[0][0][0];
     const double htn = half(tn), hten = half(ten), htv = half(tv), htev = half(tev);
     const double htnv = half(tnv), hte = half(te);
     double ta = te - htn + hten - htv + htev - tnv + tnve;
     double tb = tv - htn + htnv - hte + htev - ten + tnve;
     double tc = tn - hte + hten - htv + htnv - tev + tnve;
-    double t2 = v * v * o.dsum * 9.0;
+    double t2 = c.t3();
     double dab = ta - tb, dbc = tb - tc, dac = ta - tc;
     double t3 = o.dz2dx2 * (dab * dab);
     t3 += o.dz2dy2 * (dbc * dbc);
@@ -194,7 +257,9 @@ __device__ __forceinline__ double node_update3d(double tv, double te, double tn,
 struct Sweep3Args {
   double* tt;
   uint8_t* rec;
-  const double* slow;
+  Coef3 C;              // precomputed coefficients (COEF variant)
+  const double* slow;   // slowness cells (cell variant)
+  const int* no_skip;  // set by coef3d_kernel when the all-Big skip is not exact
   unsigned* progress;
   unsigned* ticket;
   int* status;
@@ -224,7 +289,7 @@ __device__ __forceinline__ bool wait_geq(const unsigned* p, unsigned target, int
   }
 }
 
-template <bool GRAD>
+template <bool GRAD, bool COEF>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     sweep3d_kernel(const Sweep3Args A) {
   const int lane = threadIdx.x & 31;
@@ -284,7 +349,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     const int k = sy > 0 ? K * kPK + lk : K * kPK + (kPK - 1) - lk;
     const bool in_grid = j < A.NX && k < A.NY;
     const bool frozen_jk = (j == (sx > 0 ? 0 : A.NX - 1)) || (k == (sy > 0 ? 0 : A.NY - 1));
-    // Cell indices around the column, upwind cell first (see node_update3d).
+    // Offsets of the coefficient reads that depend on the column only (see
+    // Coef3): j1, k1 are the upwind cell indices of the reference.
+    const int j1 = sx > 0 ? j - 1 : j, k1 = sy > 0 ? k - 1 : k;
+    const long long jk = (long long)j * A.NY + k;
+    const long long j1k = (long long)j1 * A.NY + k, jk1 = (long long)j * A.NY + k1;
+    const long long j1k1 = (long long)j1 * A.NY + k1;
+    // Slowness cell offsets around the column, upwind cell first (CoefCells).
     const int jm = imax(j - 1, 0), jp = imin(j, A.NX - 2);
     const int km = imax(k - 1, 0), kp = imin(k, A.NY - 2);
     const long long NYc = A.ny, NXYc = (long long)A.nx * A.ny;
@@ -292,9 +363,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     const long long ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
     double* tts = A.tt + (long long)src * A.nodes;
     uint8_t* recs = GRAD ? A.rec + (long long)src * A.nodes : nullptr;
-    const long long jk = (long long)j * A.NY + k;
     const long long dj = (long long)sx * A.NY, dk = sy;
     const long long di = (long long)sz * NXY;
+    const bool may_skip = *A.no_skip == 0;
+    const long long big_bits = __double_as_longlong(kBig);
 
     double r1 = 0.0, r2 = 0.0, r3 = 0.0;
     constexpr int kChunk = 4;
@@ -323,32 +395,57 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       const double u9_2 = __shfl_up_sync(0xffffffffu, r2, 9);
       const double u9_3 = __shfl_up_sync(0xffffffffu, r3, 9);
       const int r = s - lj - lk;
-      double res = 0.0;
-      if (in_grid && r >= 0 && r < A.NZ) {
-        const int i = sz > 0 ? r : A.NZ - 1 - r;
-        const long long n = (long long)i * NXY + jk;
-        const double t0 = ld_cg(tts + n);
-        res = t0;
-        if (r != 0 && !frozen_jk) {
-          const double tv = r1;
-          const double te = lj > 0 ? u8_1 : ld_cg(tts + n - dj);
-          const double tn = lk > 0 ? u1_1 : ld_cg(tts + n - dk);
-          const double tev = lj > 0 ? u8_2 : ld_cg(tts + n - di - dj);
-          const double tnv = lk > 0 ? u1_2 : ld_cg(tts + n - di - dk);
-          const double ten = (lj > 0 && lk > 0) ? u9_2 : ld_cg(tts + n - dj - dk);
-          const double tnve = (lj > 0 && lk > 0) ? u9_3 : ld_cg(tts + n - di - dj - dk);
-          const int im = imax(i - 1, 0), ip = imin(i, A.NZ - 2);
-          const long long iu = (sz > 0 ? im : ip) * NXYc, io = (sz > 0 ? ip : im) * NXYc;
-          double U[2][2][2];
-#pragma unroll
-          for (int a = 0; a < 2; ++a)
-#pragma unroll
-            for (int b = 0; b < 2; ++b)
-#pragma unroll
-              for (int c = 0; c < 2; ++c)
-                U[a][b][c] = __ldg(A.slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
+      const bool act = in_grid && r >= 0 && r < A.NZ;
+      const int i = sz > 0 ? r : A.NZ - 1 - r;
+      const long long n = (long long)i * NXY + jk;
+      const double t0 = act ? ld_cg(tts + n) : 0.0;
+      double res = t0;
+      bool upd = act && r != 0 && !frozen_jk;
+      double tv = 0.0, te = 0.0, tn = 0.0, tev = 0.0, tnv = 0.0, ten = 0.0, tnve = 0.0;
+      if (upd) {
+        tv = r1;
+        te = lj > 0 ? u8_1 : ld_cg(tts + n - dj);
+        tn = lk > 0 ? u1_1 : ld_cg(tts + n - dk);
+        tev = lj > 0 ? u8_2 : ld_cg(tts + n - di - dj);
+        tnv = lk > 0 ? u1_2 : ld_cg(tts + n - di - dk);
+        ten = (lj > 0 && lk > 0) ? u9_2 : ld_cg(tts + n - dj - dk);
+        tnve = (lj > 0 && lk > 0) ? u9_3 : ld_cg(tts + n - di - dj - dk);
+        // A node whose value and 7 upwind neighbours all still hold Big keeps
+        // Big (every operator then returns at least Big; coef3d_kernel checks
+        // the scale condition that makes this exact).
+        if (may_skip) {
+          const long long b = __double_as_longlong(t0);
+          const bool all_big = b == big_bits && __double_as_longlong(tv) == b &&
+                               __double_as_longlong(te) == b && __double_as_longlong(tn) == b &&
+                               __double_as_longlong(tev) == b && __double_as_longlong(tnv) == b &&
+                               __double_as_longlong(ten) == b && __double_as_longlong(tnve) == b;
+          upd = !all_big;
+        }
+      }
+      if (__any_sync(0xffffffffu, upd)) {
+        if (upd) {
           uint8_t code = 0;
-          res = node_update3d<GRAD>(tv, te, tn, tev, ten, tnv, tnve, t0, U, o, sz, sx, sy, code);
+          if (COEF) {
+            const long long i0 = (long long)i * NXY;
+            const long long i1 = (long long)(sz > 0 ? i - 1 : i) * NXY;
+            const CoefArrays cp{A.C,      i1 + jk,   i0 + j1k,   i0 + jk1,
+                                i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
+            res = node_update3d<GRAD>(tv, te, tn, tev, ten, tnv, tnve, t0, cp, o, sz, sx, sy,
+                                      code);
+          } else {
+            const int im = imax(i - 1, 0), ip = imin(i, A.NZ - 2);
+            const long long iu = (sz > 0 ? im : ip) * NXYc, io = (sz > 0 ? ip : im) * NXYc;
+            CoefCells cp{{}, o};
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+              for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int c = 0; c < 2; ++c)
+                  cp.U[a][b][c] = __ldg(A.slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
+            res = node_update3d<GRAD>(tv, te, tn, tev, ten, tnv, tnve, t0, cp, o, sz, sx, sy,
+                                      code);
+          }
           if (!deq(res, t0)) {
             tts[n] = res;
             if (GRAD) recs[n] = code;
@@ -381,6 +478,69 @@ __global__ void fill3d_kernel(double* tt, uint8_t* rec, long long n) {
        q += (long long)gridDim.x * blockDim.x) {
     tt[q] = kBig;
     if (rec) rec[q] = 13;
+  }
+}
+
+// Operator coefficients (see Coef3), one thread per node-shaped index.
+// Also checks that min(slowness) * min(spacing) >= 1e-9: then a Big-valued
+// neighbourhood provably stays Big (every operator exceeds Big by at least
+// about slowness * spacing / 2, far above the rounding of Big), which makes
+// the sweep's skip of such nodes exact; otherwise the skip is disabled.
+__global__ void coef3d_kernel(const double* slow, int nz, int nx, int ny, Ops3 o, Coef3 C,
+                              bool write, int* no_skip) {
+  const int NX = nx + 1, NY = ny + 1;
+  const long long n_nodes = (long long)(nz + 1) * NX * NY;
+  const double hmin = fmin(o.dz, fmin(o.dx, o.dy));
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_nodes;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q / ((long long)NX * NY));
+    const int j = (int)((q / NY) % NX);
+    const int k = (int)(q % NY);
+    const int im = imax(i - 1, 0), ip = imin(i, nz - 1);
+    const int jm = imax(j - 1, 0), jp = imin(j, nx - 1);
+    const int km = imax(k - 1, 0), kp = imin(k, ny - 1);
+#define S(a, b, c) __ldg(slow + ((long long)(a)*nx + (b)) * ny + (c))
+    double v;
+    if (!write) {
+      if (i < nz && j < nx && k < ny && !(S(i, j, k) * hmin >= 1e-9)) atomicOr(no_skip, 1);
+      continue;
+    }
+    if (i < nz) {
+      v = pmin(pmin(S(i, jm, km), S(i, jm, kp)), pmin(S(i, jp, km), S(i, jp, kp)));
+      C.z1[q] = o.dz * v;
+    }
+    if (j < nx) {
+      v = pmin(pmin(S(im, j, km), S(ip, j, km)), pmin(S(im, j, kp), S(ip, j, kp)));
+      C.x1[q] = o.dx * v;
+    }
+    if (k < ny) {
+      v = pmin(pmin(S(im, jm, k), S(im, jp, k)), pmin(S(ip, jm, k), S(ip, jp, k)));
+      C.y1[q] = o.dy * v;
+    }
+    if (i < nz && j < nx) {
+      v = pmin(S(i, j, km), S(i, j, kp));
+      C.zxa[q] = o.dx * v;
+      C.zxb[q] = o.dz * v;
+      C.zxq[q] = times4(v * v) * o.szx;
+    }
+    if (i < nz && k < ny) {
+      v = pmin(S(i, jm, k), S(i, jp, k));
+      C.zya[q] = o.dy * v;
+      C.zyb[q] = o.dz * v;
+      C.zyq[q] = times4(v * v) * o.szy;
+    }
+    if (j < nx && k < ny) {
+      v = pmin(S(im, j, k), S(ip, j, k));
+      C.xya[q] = o.dy * v;
+      C.xyb[q] = o.dx * v;
+      C.xyq[q] = times4(v * v) * o.sxy;
+    }
+    if (i < nz && j < nx && k < ny) {
+      v = S(i, j, k);
+      C.t3[q] = v * v * o.dsum * 9.0;
+      if (!(v * hmin >= 1e-9)) atomicOr(no_skip, 1);
+    }
+#undef S
   }
 }
 
@@ -436,9 +596,9 @@ __global__ void grad3d_kernel(const double* tt, const uint8_t* rec, const Source
     const int code = rec[q];
     const int cz = code / 9 - 1, cx = (code / 3) % 3 - 1, cy = code % 3 - 1;
     const double tq = tt[q];
-    if (cz != 0) g0 = (double)cz * (tq - tt[q - cz * NXY]) / o.dz;
-    if (cx != 0) g1 = (double)cx * (tq - tt[q - (long long)cx * NY]) / o.dx;
-    if (cy != 0) g2 = (double)cy * (tq - tt[q - cy]) / o.dy;
+    if (cz != 0) g0 = div_by((double)cz * (tq - tt[q - cz * NXY]), o.rdz);
+    if (cx != 0) g1 = div_by((double)cx * (tq - tt[q - (long long)cx * NY]), o.rdx);
+    if (cy != 0) g2 = div_by((double)cy * (tq - tt[q - cy]), o.rdy);
     const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
     if (gn > 0.0) {
       g0 /= gn;
@@ -467,7 +627,7 @@ __global__ void pencil_order_kernel(int PJ, int PK, int* order) {
 // ---------------------------------------------------------------- host side --
 
 struct Layout3 {
-  size_t status, params, src, order, progress, rec, total;
+  size_t status, params, src, order, progress, coef, rec, total;
 };
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -477,7 +637,7 @@ static Layout3 layout3(int nz, int nx, int ny, int nsrc, int grad) {
   const size_t nodes = (size_t)(nz + 1) * (nx + 1) * (ny + 1);
   Layout3 L;
   size_t off = 0;
-  L.status = off;  // int status; unsigned ticket
+  L.status = off;  // int status; unsigned ticket; int no_skip
   off = align_up(off + 16);
   L.params = off;
   off = align_up(off + sizeof(Source3) * (size_t)nsrc);
@@ -487,6 +647,8 @@ static Layout3 layout3(int nz, int nx, int ny, int nsrc, int grad) {
   off = align_up(off + sizeof(int) * (size_t)PJ * PK);
   L.progress = off;
   off = align_up(off + sizeof(unsigned) * (size_t)PJ * PK * nsrc);
+  L.coef = off;
+  off = align_up(off + sizeof(double) * nodes * kNumCoef);
   L.rec = off;
   if (grad) off = align_up(off + nodes * (size_t)nsrc);
   L.total = off;
@@ -541,12 +703,25 @@ extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, d
   uint8_t* rec = grad ? (uint8_t*)(ws + L.rec) : nullptr;
   int* status = (int*)(ws + L.status);
   unsigned* ticket = (unsigned*)(ws + L.status + 4);
+  int* no_skip = (int*)(ws + L.status + 8);
+  Coef3 C;
+  {
+    double* c = (double*)(ws + L.coef);
+    double** fields[kNumCoef] = {&C.z1,  &C.x1,  &C.y1,  &C.zxa, &C.zxb, &C.zxq, &C.zya,
+                                 &C.zyb, &C.zyq, &C.xya, &C.xyb, &C.xyq, &C.t3};
+    for (int f = 0; f < kNumCoef; ++f) *fields[f] = c + (size_t)f * nodes;
+  }
 
   FTEIK_CHECK(cudaMemsetAsync(ws + L.status, 0, 16, st));
   FTEIK_CHECK(cudaMemsetAsync(progress, 0, sizeof(unsigned) * (size_t)PJ * PK * nsrc, st));
   FTEIK_CHECK(cudaMemcpyAsync(src_dev, sources, sizeof(double) * 3 * (size_t)nsrc,
                               cudaMemcpyHostToDevice, st));
   pencil_order_kernel<<<(PJ * PK + 127) / 128, 128, 0, st>>>(PJ, PK, order);
+  // Coefficient arrays pay off when enough sources share them (they stay in
+  // L2 across the sources of a pencil); a few sources read the slowness cells.
+  const long long opt_coef = option_value(kOptSweepCoef);
+  const bool use_coef = opt_coef < 0 ? nsrc >= kCoefMinSources : opt_coef != 0;
+  coef3d_kernel<<<grid_for(nodes, 256), 256, 0, st>>>(slow, nz, nx, ny, o, C, use_coef, no_skip);
   const long long ntot = nodes * nsrc;
   fill3d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
   init3d_kernel<<<(nsrc + 63) / 64, 64, 0, st>>>(slow, src_dev, nsrc, nz, nx, ny, o, tt, nodes,
@@ -556,7 +731,9 @@ extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, d
     Sweep3Args A;
     A.tt = tt;
     A.rec = rec;
+    A.C = C;
     A.slow = slow;
+    A.no_skip = no_skip;
     A.progress = progress;
     A.ticket = ticket;
     A.status = status;
@@ -578,22 +755,18 @@ extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, d
     A.spin_limit = spin_limit > 0 ? spin_limit : (1LL << 25);
     A.o = o;
     const long long items = (long long)nepochs * PJ * PK * nsrc;
-    int blocks;
-    if (grad) {
-      blocks = resident_blocks((const void*)sweep3d_kernel<true>, kWarpsPerBlock * 32);
-    } else {
-      blocks = resident_blocks((const void*)sweep3d_kernel<false>, kWarpsPerBlock * 32);
-    }
+    const void* kern = grad ? (use_coef ? (const void*)sweep3d_kernel<true, true>
+                                        : (const void*)sweep3d_kernel<true, false>)
+                            : (use_coef ? (const void*)sweep3d_kernel<false, true>
+                                        : (const void*)sweep3d_kernel<false, false>);
+    int blocks = resident_blocks(kern, kWarpsPerBlock * 32);
     const long long need = (items + kWarpsPerBlock - 1) / kWarpsPerBlock;
     if (need < blocks) blocks = (int)need;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     timing_events(&ev0, &ev1);
     if (ev0) FTEIK_CHECK(cudaEventRecord(ev0, st));
-    if (grad)
-      sweep3d_kernel<true><<<blocks, kWarpsPerBlock * 32, 0, st>>>(A);
-    else
-      sweep3d_kernel<false><<<blocks, kWarpsPerBlock * 32, 0, st>>>(A);
-    FTEIK_CHECK(cudaGetLastError());
+    void* args[] = {(void*)&A};
+    FTEIK_CHECK(cudaLaunchKernel(kern, dim3(blocks), dim3(kWarpsPerBlock * 32), args, 0, st));
     if (ev1) FTEIK_CHECK(cudaEventRecord(ev1, st));
   }
   if (grad) {

@@ -61,6 +61,10 @@ int grid_for(long long n, int threads) {
   return (int)blocks;
 }
 
+static long long g_options[kOptCount] = {-1};
+
+long long option_value(int opt) { return (opt >= 0 && opt < kOptCount) ? g_options[opt] : -1; }
+
 static thread_local bool g_timing = false;
 static thread_local cudaEvent_t g_ev[2] = {nullptr, nullptr};
 
@@ -84,6 +88,15 @@ __global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
 }  // namespace fteik
 
 using namespace fteik;
+
+extern "C" int fteik_set_option(const char* name, long long value) {
+  if (!name) return kInvalidArgument;
+  if (std::strcmp(name, "sweep_coef") == 0) {
+    g_options[kOptSweepCoef] = value < 0 ? -1 : (value ? 1 : 0);
+    return kOk;
+  }
+  return kInvalidArgument;
+}
 
 extern "C" int fteik_kernel_timing(int on) {
   g_timing = on != 0;

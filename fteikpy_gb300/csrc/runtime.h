@@ -27,4 +27,11 @@ int grid_for(long long n, int threads);
 // 3D solve records around its sweep kernel on the launching stream; else null.
 void timing_events(cudaEvent_t* start, cudaEvent_t* stop);
 
+// Tuning options (fteik_set_option); -1 = automatic.
+enum Option : int {
+  kOptSweepCoef = 0,  // 3D sweep coefficients: 1 precomputed arrays, 0 slowness cells
+  kOptCount = 1,
+};
+long long option_value(int opt);
+
 }  // namespace fteik

@@ -41,6 +41,11 @@ const char* fteik_last_error(void);
  * kernel's duration. fteik_fp64_peak times a DFMA loop (nblocks x 256 threads,
  * 4 chains each; `scratch` holds nblocks*256 doubles) and returns FLOP/s. */
 int fteik_kernel_timing(int on);
+/* Tuning knobs (no counterpart in the reference). "sweep_coef": -1 chooses
+ * automatically, 0 makes the 3D sweep derive its slowness factors from the
+ * 8 cells around each node, 1 makes it read precomputed coefficient arrays
+ * (faster for batches of sources, which reuse them). Results are identical. */
+int fteik_set_option(const char* name, long long value);
 int fteik_last_sweep_ms(float* ms);
 int fteik_fp64_peak(double* scratch, int nblocks, int iters, double* flops_per_s, void* stream);
 

@@ -179,6 +179,9 @@ def test_golden_solve_and_interp(nd, golden2d, golden3d):
         ((40, 33, 47), (10.0, 10.0, 10.0), 5, 2, 3),
         ((25, 9, 70), (7.0, 13.0, 5.0), 2, 1, 4),
         ((30, 40, 24), (10.0, 10.0, 10.0), 1, 0, 5),
+        # micrometre spacing: slowness x spacing < 1e-9 disables the Big skip
+        ((10, 12, 9), (1e-6, 2e-6, 1.5e-6), 2, 2, 6),
+        ((64, 20, 33), (5.0, 5.0, 5.0), 3, 2, 7),
     ],
 )
 def test_solve3d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed):
@@ -312,3 +315,24 @@ def test_torch_cuda_grid_is_used_in_place():
     a = fp.Eikonal3D(vt, (10.0, 10.0, 10.0)).solve([0.0, 30.0, 40.0])
     b = fp.Eikonal3D(v, (10.0, 10.0, 10.0)).solve([0.0, 30.0, 40.0])
     assert bitwise(a.grid, b.grid)
+
+
+@pytest.mark.parametrize("coef", [0, 1])
+def test_solve3d_both_coefficient_sources(coef):
+    """The sweep's slowness factors read from precomputed arrays or derived
+    from the slowness cells give the same bits."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.fteik_set_option(b"sweep_coef", coef) == 0
+    try:
+        rng = np.random.default_rng(21)
+        shape, d = (20, 26, 30), (9.0, 10.0, 11.0)
+        v = layered3d(shape, 21)
+        src = rand_sources(rng, shape, d, 3, np.zeros(3))
+        tt_o, tg_o, _ = O.solve3d(1.0 / v, d, src, 2, True)
+        tts = fp.Eikonal3D(v, d).solve(src, nsweep=2, return_gradient=True)
+        assert bitwise(np.stack([t.grid for t in tts]), tt_o)
+        assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)
+    finally:
+        lib.fteik_set_option(b"sweep_coef", -1)

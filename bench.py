@@ -273,6 +273,250 @@ def workload_config():
     }
 
 
+def run_config1(args):
+    """Plain 2D solve (the reference's CPU-runnable case): 200 x 300 cells at
+    10 m, v(z) = 1500 + 0.6 z times (1 + 0.1 p), p seeded N(0,1) noise smoothed
+    with sigma = 8 cells and rescaled to [-1, 1]; source (5.3, 1234.7), nsweep=2.
+    Reports the GPU and CPU-oracle times, their parity, and the error of the
+    p = 0 model against the analytic linear-gradient traveltime."""
+    import torch
+
+    import fteikpy_gb300 as fp
+    from oracle import oracle as O
+    from scipy.ndimage import gaussian_filter
+
+    nz, nx, d = 200, 300, (10.0, 10.0)
+    rng = np.random.default_rng(1)
+    p = gaussian_filter(rng.standard_normal((nz, nx)), 8.0)
+    p = 2.0 * (p - p.min()) / (p.max() - p.min()) - 1.0
+    zc = (np.arange(nz) + 0.5) * d[0]
+    v0 = (1500.0 + 0.6 * zc)[:, None] * np.ones((nz, nx))
+    v = v0 * (1.0 + 0.1 * p)
+    src = np.array([5.3, 1234.7])
+    eik = fp.Eikonal2D(v, d)
+    for _ in range(max(args.warmup, 1)):
+        eik.solve(src, nsweep=2)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        tt = eik.solve(src, nsweep=2)
+        g = tt.grid
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    tto, _, _ = O.solve2d(1.0 / v, d, [src], 2, False, nthreads=1)
+    cpu = time.perf_counter() - t0
+    same = bool(np.array_equal(g, tto[0]))
+    # analytic linear-gradient traveltime for p = 0 (velocity at cell centres)
+    t_lin = fp.Eikonal2D(v0, d).solve(src, nsweep=2).grid
+    gz = 0.6
+    zn = np.arange(nz + 1)[:, None] * d[0]
+    xn = np.arange(nx + 1)[None, :] * d[1]
+    r2 = (zn - src[0]) ** 2 + (xn - src[1]) ** 2
+    vs, vn = 1500.0 + gz * src[0], 1500.0 + gz * zn
+    t_ana = np.arccosh(1.0 + gz**2 * r2 / (2.0 * vs * vn)) / gz
+    far = r2 > (5 * d[0]) ** 2
+    rel = np.abs(t_lin - t_ana)[far] / t_ana[far]
+    print(json.dumps({
+        "config": 1,
+        "metric": "2D plain solve time (200x300, nsweep=2, one off-grid source)",
+        "value": 1e3 * float(np.median(times)), "unit": "ms", "higher_is_better": False,
+        "cpu_baseline": {"value": 1e3 * cpu, "unit": "ms", "cores": 1, "kind": "port",
+                         "sample": "the same solve, C oracle, 1 thread"},
+        "parity_bitwise_vs_oracle": same,
+        "analytic_linear_gradient_rel_err": {"max": float(rel.max()), "median": float(np.median(rel)),
+                                             "excluding": "nodes within 5 cells of the source"},
+        "note": "the reference's 2D sweep is one serial dependence chain; a single 2D source "
+                "runs on one GPU thread",
+    }))
+    return 0
+
+
+def run_config2(args):
+    """Plain 3D solve: one seeded off-grid surface source on the 150 x 200 x 200
+    layered model at 10 m, nsweep=2 with gradients, then traveltimes at 10,000
+    seeded points and 400 rays to seeded surface receivers, through the drop-in
+    API (results copied to the host)."""
+    import torch
+
+    import fteikpy_gb300 as fp
+    from oracle import oracle as O
+
+    shape = (150, 200, 200)
+    v = layered_model(shape)
+    rng = np.random.default_rng(2)
+    ext = np.array(shape) * np.array(D)
+    src = np.array([0.0, rng.uniform(0.2, 0.8) * ext[1], rng.uniform(0.2, 0.8) * ext[2]])
+    pts = rng.uniform([0.0, 0.0, 0.0], ext, (10000, 3))
+    rec = np.column_stack([np.zeros(NREC), rng.uniform(0, ext[1], NREC), rng.uniform(0, ext[2], NREC)])
+    eik = fp.Eikonal3D(v, D)
+
+    def step():
+        tt = eik.solve(src, nsweep=NSWEEP, return_gradient=True)
+        a = tt(pts)
+        rays = tt.raytrace(rec)
+        return tt, a, rays
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        tt, a, rays = step()
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    tto, tgo, vzo = O.solve3d(1.0 / v, D, [src], NSWEEP, True)
+    ax = O.axes(tto.shape[1:], D, np.zeros(3))
+    ao = O.vinterp(ax, tto[0], pts, src, vzo[0])
+    max_dist = 2.0 * sum((n * h) ** 2 for n, h in zip(tto.shape[1:], D)) ** 0.5
+    rays_o = O.raytrace(ax, tgo[0], rec, src, min(D), int(max_dist / min(D)), False)
+    cpu = time.perf_counter() - t0
+    same = bool(np.array_equal(tt.grid, tto[0]) and np.array_equal(a, ao)
+                and all(np.array_equal(x, y) for x, y in zip(rays, rays_o)))
+    print(json.dumps({
+        "config": 2,
+        "metric": "plain 3D solve + 10,000 traveltime queries + 400 rays (150x200x200, nsweep=2)",
+        "value": 1e3 * float(np.median(times)), "unit": "ms", "higher_is_better": False,
+        "cell_updates_per_s": updates_per_source(shape) / float(np.median(times)),
+        "cpu_baseline": {"value": 1e3 * cpu, "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "the same step with the C oracle (the solve is one source: 1 thread)"},
+        "parity_bitwise_vs_oracle": same,
+    }))
+    return 0
+
+
+def tomography_models(shape=(96, 128, 128), d=D, seed=5):
+    """Linear-gradient starting model v(z) = 1500 + 0.6 z and the true model:
+    the same times (1 + 0.08 exp(-r^2 / (2 * 150 m^2))), a Gaussian anomaly of
+    radius 150 m centred at a seeded point in the middle of the grid."""
+    rng = np.random.default_rng(seed)
+    ext = np.array(shape) * np.array(d)
+    zc, xc, yc = [(np.arange(n) + 0.5) * h for n, h in zip(shape, d)]
+    v0 = (1500.0 + 0.6 * zc)[:, None, None] * np.ones(shape)
+    c = ext * rng.uniform([0.4, 0.35, 0.35], [0.6, 0.65, 0.65])
+    r2 = ((zc - c[0])[:, None, None] ** 2 + (xc - c[1])[None, :, None] ** 2
+          + (yc - c[2])[None, None, :] ** 2)
+    return v0, v0 * (1.0 + 0.08 * np.exp(-r2 / (2.0 * 150.0**2)))
+
+
+def run_config5(args):
+    """Adjoint gradient for tomography: 96 x 128 x 128 at 10 m, 64 surface
+    sources x 400 surface receivers, loss = 0.5 sum((T_pred - T_obs)^2) with
+    T_obs from the true model; forward and adjoint through the autograd
+    function, the gradient checked by central differences (relative step 1e-6)
+    on 50 seeded cells through the C oracle."""
+    import torch
+
+    import fteikpy_gb300 as fp
+    from fteikpy_gb300._solver import solve3d_device
+    from oracle import oracle as O
+
+    shape = (96, 128, 128)
+    v0, vt = tomography_models(shape)
+    src = surface_sources(shape, n_side=8, seed=7)
+    rec = surface_receivers(shape, n=NREC, seed=11)
+    dev = torch.device("cuda", 0)
+    t_obs = fp.traveltimes(torch.tensor(vt, device=dev), D, src, rec, NSWEEP).detach()
+    vel = torch.tensor(v0, device=dev)
+
+    def fwd_plain():
+        slow = 1.0 / vel
+        return solve3d_device(slow, D, src, NSWEEP, False)[0]
+
+    def step():
+        x = vel.clone().requires_grad_(True)
+        T = fp.traveltimes(x, D, src, rec, NSWEEP)
+        loss = 0.5 * ((T - t_obs) ** 2).sum()
+        e_mid.record()
+        loss.backward()
+        return x.grad, loss, T
+
+    e0, e_mid, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    for _ in range(max(args.warmup, 1)):
+        fwd_plain()
+        step()
+    torch.cuda.synchronize()
+    plain_ms, fwd_ms, bwd_ms = [], [], []
+    for _ in range(max(args.steps, 1)):
+        e0.record()
+        fwd_plain()
+        e1.record()
+        torch.cuda.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+        e0.record()
+        g, loss, T = step()
+        e1.record()
+        torch.cuda.synchronize()
+        fwd_ms.append(e0.elapsed_time(e_mid))
+        bwd_ms.append(e_mid.elapsed_time(e1))
+    g = g.cpu().numpy()
+    T = T.detach().cpu().numpy()
+    t_obs_h = t_obs.cpu().numpy()
+    plain, fwd, bwd = (float(np.median(x)) for x in (plain_ms, fwd_ms, bwd_ms))
+
+    def oracle_times(v):
+        tt, _, vz = O.solve3d(1.0 / v, D, src, NSWEEP, False)
+        ax = O.axes(tt.shape[1:], D, np.zeros(3))
+        return np.stack([O.vinterp(ax, tt[s], rec, src[s], vz[s]) for s in range(len(src))])
+
+    # CPU: the oracle's forward and its sequential reverse-mode adjoint, which
+    # the GPU gradient must equal on every cell
+    q0 = time.perf_counter()
+    t_oracle = oracle_times(v0)
+    cpu_fwd = time.perf_counter() - q0
+    q0 = time.perf_counter()
+    s0 = 1.0 / v0
+    g_oracle = -O.adjoint3d(s0, D, src, NSWEEP, rec, t_oracle - t_obs_h) * s0 * s0
+    cpu_adj = time.perf_counter() - q0
+    gmax = float(np.abs(g).max())
+    # central differences (relative step 1e-6) through the oracle's solve on
+    # seeded cells whose derivative is at least 1e-4 of the largest (smaller
+    # ones drown in the rounding of the differences)
+    rng = np.random.default_rng(3)
+    pool = np.flatnonzero(np.abs(g.ravel()) >= 1e-4 * gmax)
+    cells = rng.choice(pool, min(args.fd_cells, len(pool)), replace=False)
+    rows, fds = [], []
+    for c in cells:
+        idx = np.unravel_index(c, shape)
+        h = 1e-6 * v0[idx]
+        vp = v0.copy()
+        vp[idx] += h
+        vm = v0.copy()
+        vm[idx] -= h
+        tp, tm = oracle_times(vp), oracle_times(vm)
+        # L(v+h) - L(v-h) summed term by term as 0.5 (tp - tm)(tp + tm - 2 t_obs):
+        # the same difference without cancelling two losses ~1e8 times larger
+        fd = float(np.sum(0.5 * (tp - tm) * (tp + tm - 2.0 * t_obs_h))) / (2.0 * h)
+        fds.append(fd)
+        rows.append(abs(fd - g[idx]) / abs(fd))
+    rows = np.array(rows)
+    if args.dump:
+        np.savez_compressed(args.dump, grad=g, grad_oracle=g_oracle, cells=cells, fd=np.array(fds),
+                            v0=v0, t_obs=t_obs_h, t_pred=T)
+    print(json.dumps({
+        "config": 5,
+        "metric": "adjoint d(loss)/d(velocity), 96x128x128, 64 sources x 400 receivers, nsweep=2",
+        "value": fwd + bwd, "unit": "ms", "higher_is_better": False,
+        "forward_plain_ms": plain, "forward_with_tape_ms": fwd, "adjoint_ms": bwd,
+        "adjoint_over_forward": bwd / plain, "forward_plus_adjoint_over_forward": (fwd + bwd) / plain,
+        "forward_bitwise_vs_oracle": bool(np.array_equal(T, t_oracle)),
+        "adjoint_vs_oracle_adjoint_max_abs_over_gmax": float(np.abs(g - g_oracle).max() / gmax),
+        "fd": {"cells": int(len(cells)), "rel_step": 1e-6,
+               "selection": "seeded, |grad| >= 1e-4 max|grad|",
+               "rel_err_median": float(np.median(rows)) if len(rows) else None,
+               "rel_err_p90": float(np.quantile(rows, 0.9)) if len(rows) else None,
+               "rel_err_max": float(rows.max()) if len(rows) else None,
+               "cells_within_1e-6": int((rows <= 1e-6).sum()),
+               "cells_within_1e-4": int((rows <= 1e-4).sum())},
+        "cpu_baseline": {"value": 1e3 * (cpu_fwd + cpu_adj), "unit": "ms",
+                         "cores": os.cpu_count(), "kind": "port",
+                         "sample": "one forward + adjoint with the C oracle (OpenMP over sources)",
+                         "forward_ms": 1e3 * cpu_fwd, "adjoint_ms": 1e3 * cpu_adj},
+    }))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -283,14 +527,27 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end API timing")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-source-per-launch timing")
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 5],
+                    help="1: plain 2D solve, 2: plain 3D solve + queries + rays, 3: batched "
+                         "(default), 5: adjoint gradient")
+    ap.add_argument("--fd-cells", type=int, default=50,
+                    help="cells of the finite-difference check of --config 5")
+    ap.add_argument("--dump", default=None,
+                    help="--config 5: save the gradient and the finite differences (.npz)")
     ap.add_argument("--small", action="store_true",
-                    help="profiling case: 8 sources on a 64x128x128 grid (inputs still > L2)")
+                    help="profiling case: 32 sources on a 64x128x128 grid (277 MB of traveltimes, > L2)")
     args = ap.parse_args()
     if args.small:
         global SHAPE, NSRC
-        SHAPE, NSRC = (64, 128, 128), 8
+        SHAPE, NSRC = (64, 128, 128), 32
     if args.impl == "reference":
         return run_reference(args)
+    if args.config in (1, 2, 5):
+        import torch
+
+        if torch.cuda.is_available():
+            torch.cuda.set_device(0)
+        return {1: run_config1, 2: run_config2, 5: run_config5}[args.config](args)
 
     import torch
 

@@ -11,6 +11,7 @@ from ._build import build
 from ._grid import Grid2D, Grid3D, TraveltimeGrid2D, TraveltimeGrid3D
 from ._helpers import get_num_threads, set_num_threads
 from ._solver import Eikonal2D, Eikonal3D
+from ._adjoint import converged, traveltimes
 
 __all__ = [
     "Eikonal2D",
@@ -20,6 +21,8 @@ __all__ = [
     "TraveltimeGrid2D",
     "TraveltimeGrid3D",
     "build",
+    "converged",
+    "traveltimes",
     "get_num_threads",
     "set_num_threads",
     "__version__",

@@ -32,6 +32,16 @@ SIGNATURES = {
     "fteik3d_solve_async": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P]),
     "fteik_workspace_status": (_I, [_P, _P]),
     "fteik3d_solve_noalloc": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _LL, _P]),
+    "fteik3d_adjoint_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
+    "fteik3d_tape_bytes": (_SZ, [_I, _I, _I, _I, _I]),
+    "fteik3d_solve_tape": (
+        _I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _P, _P, _SZ, _P, _SZ, _LL, _P]
+    ),
+    "fteik3d_adjoint": (
+        _I,
+        [_P, _I, _I, _I, _D, _D, _D, _I, _I, _P, _P, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _I, _P,
+         _P, _P, _SZ, _P],
+    ),
     "fteik2d_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
     "fteik2d_solve": (_I, [_P, _I, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _P]),
     "fteik_interp3d": (_I, [_P, _I, _P, _I, _P, _I, _P, _LL, _P, _I, _D, _P, _P]),

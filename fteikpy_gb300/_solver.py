@@ -142,25 +142,31 @@ class Eikonal3D(BaseGrid3D, _SolverMixin):
         return self._wrap(TraveltimeGrid3D, sources, rel, tt, ttgrad, vzero, return_gradient)
 
 
-def solve3d_device(slow, gridsize, src, nsweep=2, return_gradient=False, spin_limit=None):
+def solve3d_device(slow, gridsize, src, nsweep=2, return_gradient=False, spin_limit=None,
+                   workspace=None, record=False):
     """Batched 3D solve on device tensors: ``slow`` [nz, nx, ny] (CUDA, float64),
     ``src`` [nsrc, 3] host coordinates relative to the grid origin.
-    Returns device tensors (tt, ttgrad or None, vzero)."""
+    Returns device tensors (tt, ttgrad or None, vzero).
+
+    ``record=True`` keeps the branch record in ``workspace`` (a uint8 CUDA
+    tensor of at least ``fteik3d_workspace_bytes`` bytes) for the adjoint."""
     src = np.ascontiguousarray(np.atleast_2d(src), dtype=np.float64)
     nsrc = len(src)
     nz, nx, ny = slow.shape
-    grad = bool(return_gradient)
+    grad = 1 if return_gradient else (2 if record else 0)
     dev = slow.device
     tt = torch.empty((nsrc, nz + 1, nx + 1, ny + 1), dtype=torch.float64, device=dev)
     ttgrad = (
         torch.empty((nsrc, nz + 1, nx + 1, ny + 1, 3), dtype=torch.float64, device=dev)
-        if grad
+        if grad == 1
         else None
     )
     vzero = torch.empty(nsrc, dtype=torch.float64, device=dev)
     lib = _lib.load()
     nbytes = lib.fteik3d_workspace_bytes(nz, nx, ny, nsrc, int(grad))
-    ws = _device.workspace("solve3d", nbytes)
+    ws = workspace if workspace is not None else _device.workspace("solve3d", nbytes)
+    if ws.numel() < nbytes:
+        raise ValueError("workspace too small")
     rc = lib.fteik3d_solve(
         _device.ptr(slow), nz, nx, ny, *[float(g) for g in gridsize], _device.host_ptr(src),
         nsrc, max(int(nsweep), 0), int(grad), _device.ptr(tt), _device.ptr(ttgrad),

@@ -32,74 +32,15 @@
 #include "common.cuh"
 #include "fteik_gb300.h"
 #include "runtime.h"
+#include "solve3d.cuh"
 
 namespace fteik {
 
-constexpr int kPJ = 4;  // pencil width along x (j)
-constexpr int kPK = 8;  // pencil width along y (k)
 constexpr int kLag = kPJ + kPK - 2;
 constexpr int kWarpsPerBlock = 4;
 // Batches of at least this many sources read precomputed coefficient arrays.
 constexpr int kCoefMinSources = 4;
 
-struct Ops3 {
-  double dz, dx, dy, dz2i, dx2i, dy2i, dz2dx2, dz2dy2, dx2dy2, dsum;
-  double szx, szy, sxy;  // dz2i + dx2i, dz2i + dy2i, dx2i + dy2i
-  Recip rzx, rzy, rxy, rsum;
-  Recip rdz, rdx, rdy;  // for the gradient post-pass
-};
-
-// Per-sweep constants, _fteik3d.py:208-215.
-static Ops3 make_ops3(double dz, double dx, double dy) {
-  Ops3 o;
-  o.dz = dz;
-  o.dx = dx;
-  o.dy = dy;
-  o.dz2i = 1.0 / dz / dz;
-  o.dx2i = 1.0 / dx / dx;
-  o.dy2i = 1.0 / dy / dy;
-  o.dz2dx2 = o.dz2i * o.dx2i;
-  o.dz2dy2 = o.dz2i * o.dy2i;
-  o.dx2dy2 = o.dx2i * o.dy2i;
-  o.dsum = o.dz2i + o.dx2i + o.dy2i;
-  o.szx = o.dz2i + o.dx2i;
-  o.szy = o.dz2i + o.dy2i;
-  o.sxy = o.dx2i + o.dy2i;
-  o.rzx = make_recip(o.szx);
-  o.rzy = make_recip(o.szy);
-  o.rxy = make_recip(o.sxy);
-  o.rsum = make_recip(o.dsum);
-  o.rdz = make_recip(dz);
-  o.rdx = make_recip(dx);
-  o.rdy = make_recip(dy);
-  return o;
-}
-
-struct Source3 {
-  double zsa, xsa, ysa, vzero;
-  int zsi, xsi, ysi, pad;
-};
-
-// t_ana / t_anad, _fteik3d.py:10-35.
-__device__ __forceinline__ double t_ana3(int i, int j, int k, const Ops3& o, const Source3& s) {
-  double a = o.dz * ((double)i - s.zsa);
-  double b = o.dx * ((double)j - s.xsa);
-  double c = o.dy * ((double)k - s.ysa);
-  return s.vzero * sqrt(a * a + b * b + c * c);
-}
-__device__ __forceinline__ double t_anad3(int i, int j, int k, const Ops3& o, const Source3& s,
-                                          double& tzc, double& txc, double& tyc) {
-  double t = t_ana3(i, j, k, o, s);
-  if (t > 0.0) {
-    double tmp = s.vzero * s.vzero / t;
-    tzc = ((double)i - s.zsa) * o.dz * tmp;
-    txc = ((double)j - s.xsa) * o.dx * tmp;
-    tyc = ((double)k - s.ysa) * o.dy * tmp;
-  } else {
-    tzc = txc = tyc = 0.0;
-  }
-  return t;
-}
 
 // Plane operator of _fteik3d.py:113-117 (and its ZY / XY twins):
 //   ((p*cp + q*cq) + sqrt(q4 - prod*(ta-tb)^2)) / sum,  q4 = 4*v^2*sum
@@ -110,20 +51,6 @@ __device__ __forceinline__ double plane_op(double p, double cp, double q, double
   return div_by(num + sqrt(rad), r);
 }
 
-// Slowness-only operator coefficients, the same for every source and sweep,
-// computed once per solve by coef3d_kernel.  Node-shaped arrays with node
-// strides; the index in brackets is where the update reads them, with
-// (i1, j1, k1) the reference's upwind cell (i - sgnvz, ...):
-//   z1[i1][j][k]   = dz * min of the 4 cells of row i1 around column (j, k)
-//   x1[i][j1][k], y1[i][j][k1]: the same along x and y      (_fteik3d.py:76-102)
-//   zx?[i1][j1][k] from v = min(s[i1,j1,max(k-1,0)], s[i1,j1,min(k,ny-2)]):
-//        a = dx*v, b = dz*v, q = 4*v^2*(dz2i+dx2i)           (_fteik3d.py:109-117)
-//   zy?[i1][j][k1], xy?[i][j1][k1]: the ZY and XY planes     (_fteik3d.py:121-141)
-//   t3[i1][j1][k1] = s^2 * dsum * 9                          (_fteik3d.py:148,153)
-struct Coef3 {
-  double *z1, *x1, *y1, *zxa, *zxb, *zxq, *zya, *zyb, *zyq, *xya, *xyb, *xyq, *t3;
-};
-constexpr int kNumCoef = 13;
 
 // Where the update gets its coefficients from.  Both give the same values:
 //  * CoefArrays reads the precomputed arrays (one read each; pays off when
@@ -260,6 +187,8 @@ struct Sweep3Args {
   Coef3 C;              // precomputed coefficients (COEF variant)
   const double* slow;   // slowness cells (cell variant)
   const int* no_skip;  // set by coef3d_kernel when the all-Big skip is not exact
+  uint8_t* tape_code;   // optional: per sweep, the operator code of every change
+  double* tape_old;     // optional: per sweep, the value each change replaced
   unsigned* progress;
   unsigned* ticket;
   int* status;
@@ -449,6 +378,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           if (!deq(res, t0)) {
             tts[n] = res;
             if (GRAD) recs[n] = code;
+            if (A.tape_code) {
+              const long long tq = ((long long)e * A.nsrc + src) * A.nodes + n;
+              A.tape_code[tq] = code;
+              A.tape_old[tq] = t0;
+            }
           }
         }
       }
@@ -626,34 +560,6 @@ __global__ void pencil_order_kernel(int PJ, int PK, int* order) {
 
 // ---------------------------------------------------------------- host side --
 
-struct Layout3 {
-  size_t status, params, src, order, progress, coef, rec, total;
-};
-
-static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
-
-static Layout3 layout3(int nz, int nx, int ny, int nsrc, int grad) {
-  const int PJ = (nx + 1 + kPJ - 1) / kPJ, PK = (ny + 1 + kPK - 1) / kPK;
-  const size_t nodes = (size_t)(nz + 1) * (nx + 1) * (ny + 1);
-  Layout3 L;
-  size_t off = 0;
-  L.status = off;  // int status; unsigned ticket; int no_skip
-  off = align_up(off + 16);
-  L.params = off;
-  off = align_up(off + sizeof(Source3) * (size_t)nsrc);
-  L.src = off;
-  off = align_up(off + sizeof(double) * 3 * (size_t)nsrc);
-  L.order = off;
-  off = align_up(off + sizeof(int) * (size_t)PJ * PK);
-  L.progress = off;
-  off = align_up(off + sizeof(unsigned) * (size_t)PJ * PK * nsrc);
-  L.coef = off;
-  off = align_up(off + sizeof(double) * nodes * kNumCoef);
-  L.rec = off;
-  if (grad) off = align_up(off + nodes * (size_t)nsrc);
-  L.total = off;
-  return L;
-}
 
 }  // namespace fteik
 
@@ -664,14 +570,14 @@ extern "C" size_t fteik3d_workspace_bytes(int nz, int nx, int ny, int nsrc, int 
   return layout3(nz, nx, ny, nsrc, grad).total;
 }
 
-extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, double dz,
-                                   double dx, double dy, const double* sources, int nsrc,
-                                   int nsweep, int grad, double* tt, double* ttgrad,
-                                   double* vzero, void* workspace, size_t workspace_bytes,
-                                   long long spin_limit, void* stream) {
+static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                        double dy, const double* sources, int nsrc, int nsweep, int grad,
+                        double* tt, double* ttgrad, double* vzero, void* workspace,
+                        size_t workspace_bytes, uint8_t* tape_code, double* tape_old,
+                        long long spin_limit, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || nsweep < 0 || !slow || !sources || !tt ||
-      !vzero || !workspace || (grad && !ttgrad))
+      !vzero || !workspace || grad < 0 || grad > 2 || (grad == 1 && !ttgrad))
     return kInvalidArgument;
   if (!(dz > 1e-100 && dz < 1e100 && dx > 1e-100 && dx < 1e100 && dy > 1e-100 && dy < 1e100))
     return kInvalidArgument;
@@ -734,6 +640,8 @@ extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, d
     A.C = C;
     A.slow = slow;
     A.no_skip = no_skip;
+    A.tape_code = tape_code;
+    A.tape_old = tape_old;
     A.progress = progress;
     A.ticket = ticket;
     A.status = status;
@@ -769,12 +677,46 @@ extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, d
     FTEIK_CHECK(cudaLaunchKernel(kern, dim3(blocks), dim3(kWarpsPerBlock * 32), args, 0, st));
     if (ev1) FTEIK_CHECK(cudaEventRecord(ev1, st));
   }
-  if (grad) {
+  if (grad == 1) {
     grad3d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, params, nsrc, NZ, NX, NY, o,
                                                        ttgrad);
     FTEIK_CHECK(cudaGetLastError());
   }
   return kOk;
+}
+
+extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, double dz,
+                                   double dx, double dy, const double* sources, int nsrc,
+                                   int nsweep, int grad, double* tt, double* ttgrad,
+                                   double* vzero, void* workspace, size_t workspace_bytes,
+                                   long long spin_limit, void* stream) {
+  return solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, nsweep, grad, tt, ttgrad,
+                      vzero, workspace, workspace_bytes, nullptr, nullptr, spin_limit, stream);
+}
+
+extern "C" size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep) {
+  if (nz < 1 || nx < 1 || ny < 1 || nsrc < 1 || nsweep < 0) return 0;
+  const size_t n = (size_t)(nz + 1) * (nx + 1) * (ny + 1) * nsrc * 8 * (size_t)nsweep;
+  return n == 0 ? 256 : align_up(n) + align_up(8 * n);  // nsweep 0: a token buffer
+}
+
+extern "C" int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, double dz,
+                                  double dx, double dy, const double* sources, int nsrc,
+                                  int nsweep, double* tt, double* vzero, void* workspace,
+                                  size_t workspace_bytes, void* tape, size_t tape_bytes,
+                                  long long spin_limit, void* stream) {
+  const size_t need = fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep);
+  if (!tape || need == 0) return kInvalidArgument;
+  if (tape_bytes < need) return kWorkspaceTooSmall;
+  const size_t n = (size_t)(nz + 1) * (nx + 1) * (ny + 1) * nsrc * 8 * (size_t)nsweep;
+  uint8_t* code = (uint8_t*)tape;
+  double* old = (double*)((char*)tape + align_up(n));
+  // 255 marks "unchanged in this sweep"
+  FTEIK_CHECK(cudaMemsetAsync(code, 0xff, n, (cudaStream_t)stream));
+  int rc = solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, nsweep, 2, tt, nullptr,
+                        vzero, workspace, workspace_bytes, code, old, spin_limit, stream);
+  if (rc != kOk) return rc;
+  return fteik_workspace_status(workspace, stream);
 }
 
 extern "C" int fteik3d_solve(const double* slow, int nz, int nx, int ny, double dz, double dx,

@@ -65,8 +65,10 @@ int fteik_slowness(const double* velocity, long long n, double* slow, int* flag,
  *  slow      device [nz][nx][ny] slowness (1 / velocity), cell counts nz, nx, ny
  *  sources   HOST   [nsrc][3] source (z, x, y) relative to the grid origin
  *  tt        device [nsrc][nz+1][nx+1][ny+1] traveltimes (output)
+ *  grad      0: traveltimes only; 1: also the unit gradients; 2: traveltimes
+ *            and the branch record kept in the workspace (no gradients)
  *  ttgrad    device [nsrc][nz+1][nx+1][ny+1][3] unit gradients (output; may be
- *            NULL when grad == 0)
+ *            NULL unless grad == 1)
  *  vzero     device [nsrc] slowness at each source cell (output)
  *  workspace device scratch of at least fteik3d_workspace_bytes(...) bytes
  *  spin_limit maximum polls of one dependency wait before the kernel gives up
@@ -107,6 +109,42 @@ int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny, double dz,
                           double dy, const double* sources, int nsrc, int nsweep, int grad,
                           double* tt, double* ttgrad, double* vzero, long long spin_limit,
                           void* stream);
+
+/* ------------------------------------------------------------- 3D adjoint --
+ * No counterpart in the reference (which is not differentiable): the gradient
+ * of a loss on receiver traveltimes with respect to slowness, for tomography.
+ *
+ * fteik3d_solve_tape runs the same solve as fteik3d_solve (grad = 2: no
+ * gradients, branch record kept) and also writes a tape of every sweep: per
+ * node, the code of the operator that changed it (the reference's ttsgn
+ * encoding, _fteik3d.py:166-200; 255 = unchanged) and the value it replaced.
+ * `tape` is a device buffer of fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep)
+ * bytes (9 bytes per node, source and directional sweep).
+ *
+ * fteik3d_adjoint then differentiates exactly the computation that solve ran,
+ * sweep by sweep in reverse, so the gradient matches finite differences of
+ * the solver for any nsweep, converged or not.
+ *  slow, tt, solve_workspace, tape   the inputs and results of that solve
+ *  ax0..ax2    device node axes (lengths nz+1, nx+1, ny+1) used for the
+ *              receivers' traveltimes (apparent-velocity interpolation)
+ *  sources     device [nsrc][3] source coordinates on those axes
+ *  receivers   device [nrec][3], the same receivers for every source
+ *  grad_tt_rec device [nsrc][nrec] d(loss)/d(traveltime at receiver)
+ *  grad_slow   device [nz][nx][ny] d(loss)/d(slowness), summed over sources
+ * Deterministic (no floating-point atomics). Both calls block. */
+size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep);
+int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                       double dy, const double* sources, int nsrc, int nsweep, double* tt,
+                       double* vzero, void* workspace, size_t workspace_bytes, void* tape,
+                       size_t tape_bytes, long long spin_limit, void* stream);
+size_t fteik3d_adjoint_workspace_bytes(int nz, int nx, int ny, int nsrc);
+int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,
+                    int nsrc, int nsweep, const double* tt, const void* solve_workspace,
+                    size_t solve_workspace_bytes, const void* tape, size_t tape_bytes,
+                    const double* ax0, const double* ax1, const double* ax2,
+                    const double* sources, const double* receivers, int nrec,
+                    const double* grad_tt_rec, double* grad_slow, void* workspace,
+                    size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------- 2D solve --
  * Replaces solve2d / fteik2d / fteik2d_vectorized

@@ -243,6 +243,8 @@ static void sweep3d(double* tt, int8_t* sgn, const double* slow, double dz, doub
 
 /* fteik3d, _fteik3d.py:394-490.  slow is [nz][nx][ny] cells; tt is
  * [nz+1][nx+1][ny+1]; ttgrad (may be NULL when grad == 0) is [...][3]. */
+static int8_t* g_sgn_out = NULL; /* when set, receives the branch record of the next solve */
+
 int oracle_fteik3d(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,
                    double zsrc, double xsrc, double ysrc, int nsweep, int grad, double* tt,
                    double* ttgrad, double* vzero_out) {
@@ -300,10 +302,23 @@ int oracle_fteik3d(const double* slow, int nz, int nx, int ny, double dz, double
             g[2] /= gn;
           }
         }
+    if (g_sgn_out) memcpy(g_sgn_out, sgn, (size_t)nn * 3);
     free(sgn);
   }
   *vzero_out = vzero;
   return ST_OK;
+}
+
+/* One solve (with gradients) that also returns the branch record, the
+ * reference's ttsgn (_fteik3d.py:431-437), as int8 [nodes][3]. */
+int oracle_fteik3d_record(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                          double dy, double zsrc, double xsrc, double ysrc, int nsweep,
+                          double* tt, double* ttgrad, double* vzero, int8_t* sgn) {
+  g_sgn_out = sgn;
+  int st = oracle_fteik3d(slow, nz, nx, ny, dz, dx, dy, zsrc, xsrc, ysrc, nsweep, 1, tt, ttgrad,
+                          vzero);
+  g_sgn_out = NULL;
+  return st;
 }
 
 /* fteik3d_vectorized, _fteik3d.py:493-513: one solve per source, in
@@ -1024,4 +1039,303 @@ void oracle_ray2d(const double* z, int nz, const double* x, int nx, const double
     status[r] = ray_one(2, ax, n, grad, ends + 2 * r, src, stepsize, max_step, honor_grid,
                         rays + (long)r * max_step * 2, counts + r);
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Adjoint of the 3D solve (no counterpart in the reference)                */
+/* ------------------------------------------------------------------------ */
+/*
+ * d(loss)/d(slowness) for a loss on the traveltimes _vinterp3d gives at
+ * receivers, as the plain sequential reverse-mode derivative of
+ * oracle_fteik3d: the forward runs the reference's sweep loops unchanged and
+ * tapes, per directional sweep, every node that changed (the branch code of
+ * the winning operator, _fteik3d.py:166-200, and the value it replaced); the
+ * reverse pass walks each sweep's loop nest backwards and pushes the adjoint
+ * of every changed node to the inputs of its operator.
+ *
+ * Where the operator's slowness is a minimum over 2 or 4 cells and several
+ * distinct cells share it, each of them gets half the partial (the mean of
+ * the two one-sided derivatives, i.e. what a central difference measures).
+ *
+ * The checker for fteik3d_adjoint; finite differences of oracle_fteik3d pin it.
+ */
+
+/* partials of the operator coded (a, b, c) at node (i, j, k) in the current
+ * traveltimes; w[] indexed like the reference's neighbour names. */
+enum { W_TV, W_TE, W_TN, W_TEV, W_TEN, W_TNV, W_TNVE, W_N };
+
+static int distinct_min_cells(const double* slow, const long* c, int n, long* out, double* vmin) {
+  double m = slow[c[0]];
+  for (int q = 1; q < n; ++q)
+    if (slow[c[q]] < m) m = slow[c[q]];
+  int k = 0;
+  for (int q = 0; q < n; ++q) {
+    if (slow[c[q]] != m) continue;
+    int dup = 0;
+    for (int r = 0; r < k; ++r) dup |= out[r] == c[q];
+    if (!dup) out[k++] = c[q];
+  }
+  *vmin = m;
+  return k;
+}
+
+static void adj_push(double* tt, double* lam, double* gs, const double* slow, const dargs3_t* d,
+                     int i, int j, int k, int a, int b, int c, int nz, int nx, int ny,
+                     double lam_n) {
+  /* nz, nx, ny are NODE counts here, as in sweep3_node */
+  const long NXY = (long)nx * ny, SXY = (long)(nx - 1) * (ny - 1);
+  const int SY = ny - 1;
+#define IDX(p, q, r) ((long)(p)*NXY + (long)(q)*ny + (r))
+#define CEL(p, q, r) ((long)(p)*SXY + (long)(q)*SY + (r))
+  int tz = a, tx = b, ty = c; /* the sweep's signs where the operator uses an axis */
+  long nv = IDX(i - tz, j, k), ne = IDX(i, j - tx, k), nn = IDX(i, j, k - ty);
+  long nev = IDX(i - tz, j - tx, k), nen = IDX(i, j - tx, k - ty);
+  long nnv = IDX(i - tz, j, k - ty), nnve = IDX(i - tz, j - tx, k - ty);
+  int i1 = i - (tz > 0), j1 = j - (tx > 0), k1 = k - (ty > 0);
+  int im = imax(i - 1, 0), ip = imin(i, nz - 2);
+  int jm = imax(j - 1, 0), jp = imin(j, nx - 2);
+  int km = imax(k - 1, 0), kp = imin(k, ny - 2);
+  double w[W_N] = {0, 0, 0, 0, 0, 0, 0};
+  long cand[4], cells[4];
+  int ncell = 0;
+  double ps = 0.0, v;
+  int nnz = (a != 0) + (b != 0) + (c != 0);
+  if (nnz == 1) {
+    if (a) {
+      cand[0] = CEL(i1, jm, km); cand[1] = CEL(i1, jm, kp);
+      cand[2] = CEL(i1, jp, km); cand[3] = CEL(i1, jp, kp);
+      w[W_TV] = 1.0; ps = d->dz;
+    } else if (b) {
+      cand[0] = CEL(im, j1, km); cand[1] = CEL(ip, j1, km);
+      cand[2] = CEL(im, j1, kp); cand[3] = CEL(ip, j1, kp);
+      w[W_TE] = 1.0; ps = d->dx;
+    } else {
+      cand[0] = CEL(im, jm, k1); cand[1] = CEL(im, jp, k1);
+      cand[2] = CEL(ip, jm, k1); cand[3] = CEL(ip, jp, k1);
+      w[W_TN] = 1.0; ps = d->dy;
+    }
+    ncell = distinct_min_cells(slow, cand, 4, cells, &v);
+  } else if (nnz == 2) {
+    /* t = (p1 * x + p2 * y + sqrt(4 v^2 (p1 + p2) - p1 p2 (x - y)^2)) / (p1 + p2)
+     * with x, y the two combinations below and p1, p2 their weights */
+    double p1, p2, x, y;
+    int u1, u2, u12; /* inputs: x = u12 + u1 - u2 ... spelled out per plane */
+    if (!c) { /* ZX: x = tb = tev - te + tv (weight dz2i), y = ta = tev + te - tv (dx2i) */
+      cand[0] = CEL(i1, j1, km); cand[1] = CEL(i1, j1, kp);
+      p1 = d->dz2i; p2 = d->dx2i;
+      x = tt[nev] - tt[ne] + tt[nv]; y = tt[nev] + tt[ne] - tt[nv];
+      u1 = W_TV; u2 = W_TE; u12 = W_TEV;
+    } else if (!b) { /* ZY: x = ta = tv - tn + tnv (dz2i), y = tb = tn - tv + tnv (dy2i) */
+      cand[0] = CEL(i1, jm, k1); cand[1] = CEL(i1, jp, k1);
+      p1 = d->dz2i; p2 = d->dy2i;
+      x = tt[nv] - tt[nn] + tt[nnv]; y = tt[nn] - tt[nv] + tt[nnv];
+      u1 = W_TV; u2 = W_TN; u12 = W_TNV;
+    } else { /* XY: x = ta = te - tn + ten (dx2i), y = tb = tn - te + ten (dy2i) */
+      cand[0] = CEL(im, j1, k1); cand[1] = CEL(ip, j1, k1);
+      p1 = d->dx2i; p2 = d->dy2i;
+      x = tt[ne] - tt[nn] + tt[nen]; y = tt[nn] - tt[ne] + tt[nen];
+      u1 = W_TE; u2 = W_TN; u12 = W_TEN;
+    }
+    ncell = distinct_min_cells(slow, cand, 2, cells, &v);
+    double P = p1 + p2, dxy = x - y;
+    double R = sqrt(4.0 * v * v * P - p1 * p2 * dxy * dxy);
+    double dx_ = (p1 - p1 * p2 * dxy / R) / P; /* dt/dx */
+    double dy_ = (p2 + p1 * p2 * dxy / R) / P; /* dt/dy */
+    /* x = u1-ish: in every plane x = +u1 - u2 + u12, y = -u1 + u2 + u12 */
+    w[u1] = dx_ - dy_;
+    w[u2] = -dx_ + dy_;
+    w[u12] = dx_ + dy_;
+    ps = 4.0 * v / R;
+  } else {
+    double tv = tt[nv], te = tt[ne], tn = tt[nn], tev = tt[nev], ten = tt[nen], tnv = tt[nnv],
+           tnve = tt[nnve];
+    double ta = te - 0.5 * tn + 0.5 * ten - 0.5 * tv + 0.5 * tev - tnv + tnve;
+    double tb = tv - 0.5 * tn + 0.5 * tnv - 0.5 * te + 0.5 * tev - ten + tnve;
+    double tc = tn - 0.5 * te + 0.5 * ten - 0.5 * tv + 0.5 * tnv - tev + tnve;
+    cells[0] = CEL(i1, j1, k1);
+    ncell = 1;
+    v = slow[cells[0]];
+    double Wr = sqrt(v * v * d->dsum * 9.0 - d->dz2dx2 * (ta - tb) * (ta - tb) -
+                     d->dz2dy2 * (tb - tc) * (tb - tc) - d->dx2dy2 * (ta - tc) * (ta - tc));
+    /* t = (dz2i tb + dx2i ta + dy2i tc + Wr) / dsum */
+    double ga = (d->dx2i - (d->dz2dx2 * (ta - tb) + d->dx2dy2 * (ta - tc)) / Wr) / d->dsum;
+    double gb = (d->dz2i - (d->dz2dy2 * (tb - tc) - d->dz2dx2 * (ta - tb)) / Wr) / d->dsum;
+    double gc = (d->dy2i + (d->dz2dy2 * (tb - tc) + d->dx2dy2 * (ta - tc)) / Wr) / d->dsum;
+    /* coefficients of (tv, te, tn, tev, ten, tnv, tnve) in ta, tb, tc */
+    static const double A[3][7] = {{-0.5, 1.0, -0.5, 0.5, 0.5, -1.0, 1.0},
+                                   {1.0, -0.5, -0.5, 0.5, -1.0, 0.5, 1.0},
+                                   {-0.5, -0.5, 1.0, -1.0, 0.5, 0.5, 1.0}};
+    for (int q = 0; q < 7; ++q) w[q] = ga * A[0][q] + gb * A[1][q] + gc * A[2][q];
+    ps = 9.0 * v / Wr;
+  }
+  const long in[W_N] = {nv, ne, nn, nev, nen, nnv, nnve};
+  for (int q = 0; q < W_N; ++q)
+    if (w[q] != 0.0) lam[in[q]] += lam_n * w[q];
+  if (ncell > 1) ps *= 0.5;
+  for (int q = 0; q < ncell; ++q) gs[cells[q]] += lam_n * ps;
+#undef IDX
+#undef CEL
+}
+
+/* Partials of _vinterp3d's value at one receiver with respect to the node
+ * traveltimes (added into lam, scaled by g) and to vzero (returned). */
+static double vinterp3_adjoint(const double* x, int nx, const double* y, int ny, const double* z,
+                               int nz, const double* v, double* lam, double xq, double yq,
+                               double zq, double xs, double ys, double zs, double g) {
+  int condx = x[0] <= xq && xq <= x[nx - 1];
+  int condy = y[0] <= yq && yq <= y[ny - 1];
+  int condz = z[0] <= zq && zq <= z[nz - 1];
+  if (!(condx && condy && condz)) return 0.0;
+  int xsi = search_right_m1(x, nx, xs), ysi = search_right_m1(y, ny, ys),
+      zsi = search_right_m1(z, nz, zs);
+  int i1 = search_right_m1(x, nx, xq), j1 = search_right_m1(y, ny, yq),
+      k1 = search_right_m1(z, nz, zq);
+  double D = dist3(xs, ys, zs, xq, yq, zq);
+  if (xsi == i1 && ysi == j1 && zsi == k1) return g * D;
+  int ei = i1 == nx - 1, ej = j1 == ny - 1, ek = k1 == nz - 1;
+  double xx[2] = {x[i1], ei ? 2.0 * x[i1] - x[nx - 2] : x[i1 + 1]};
+  double yy[2] = {y[j1], ej ? 2.0 * y[j1] - y[ny - 2] : y[j1 + 1]};
+  double zz[2] = {z[k1], ek ? 2.0 * z[k1] - z[nz - 2] : z[k1 + 1]};
+  double dd[8], vv[8], ww[8];
+  long id[8];
+  for (int q = 0; q < 8; ++q) {
+    int a = q & 1, b = (q >> 1) & 1, c = q >> 2; /* corner (x, y, z) offsets */
+    int past = (a && ei) || (b && ej) || (c && ek);
+    id[q] = past ? -1 : ((long)(i1 + a) * ny + (j1 + b)) * nz + (k1 + c);
+    dd[q] = past ? 0.0 : dist3(xs, ys, zs, xx[a], yy[b], zz[c]);
+    vv[q] = past ? 1.0 : v[id[q]];
+    ww[q] = fabs((xx[1 - a] - xq) * (yy[1 - b] - yq) * (zz[1 - c] - zq));
+  }
+  for (int q = 0; q < 8; ++q)
+    if (vv[q] == 0.0) return g * D;
+  double W = fabs((xx[1] - xx[0]) * (yy[1] - yy[0]) * (zz[1] - zz[0]));
+  double vq = 0.0;
+  for (int q = 0; q < 8; ++q) vq += dd[q] / vv[q] * ww[q];
+  vq /= W;
+  /* T = D / vq; dT/dv_q = D / vq^2 * dd_q ww_q / (W v_q^2) */
+  for (int q = 0; q < 8; ++q)
+    if (id[q] >= 0) lam[id[q]] += g * D / (vq * vq) * dd[q] * ww[q] / (W * vv[q] * vv[q]);
+  return 0.0;
+}
+
+/* One source: forward with tape, then the reverse pass.  gs (cells) receives
+ * this source's d(loss)/d(slowness). */
+static int adjoint3d_one(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                         double dy, const double* src, int nsweep, const double* ax0,
+                         const double* ax1, const double* ax2, const double* rec, int nrec,
+                         const double* grec, double* gs) {
+  int NZ = nz + 1, NX = nx + 1, NY = ny + 1;
+  long nn = (long)NZ * NX * NY;
+  int nep = 8 * nsweep;
+  double* tt = (double*)malloc(sizeof(double) * nn);
+  double* tg = (double*)malloc(sizeof(double) * nn * 3);
+  double* lam = (double*)calloc((size_t)nn, sizeof(double));
+  double* old = (double*)malloc(sizeof(double) * nn * (nep ? nep : 1));
+  uint8_t* code = (uint8_t*)malloc((size_t)nn * (nep ? nep : 1));
+  int8_t* sgn = (int8_t*)calloc((size_t)nn * 3, 1);
+  double vz;
+  /* initial state: a 0-sweep solve */
+  int st = oracle_fteik3d(slow, nz, nx, ny, dz, dx, dy, src[0], src[1], src[2], 0, 0, tt, NULL,
+                          &vz);
+  if (st != ST_OK) goto done;
+  memset(code, 255, (size_t)nn * (nep ? nep : 1));
+  dargs3_t d;
+  d.dz = dz; d.dx = dx; d.dy = dy;
+  d.dz2i = 1.0 / dz / dz; d.dx2i = 1.0 / dx / dx; d.dy2i = 1.0 / dy / dy;
+  d.dz2dx2 = d.dz2i * d.dx2i; d.dz2dy2 = d.dz2i * d.dy2i; d.dx2dy2 = d.dx2i * d.dy2i;
+  d.dsum = d.dz2i + d.dx2i + d.dy2i;
+  static const int S[8][3] = {{1, 1, 1},   {1, -1, 1},  {1, 1, -1},  {1, -1, -1},
+                              {-1, 1, 1},  {-1, -1, 1}, {-1, 1, -1}, {-1, -1, -1}};
+  for (int e = 0; e < nep; ++e) {
+    int tz = S[e & 7][0], tx = S[e & 7][1], ty = S[e & 7][2];
+    int k0 = ty > 0 ? 1 : NY - 2, k1 = ty > 0 ? NY : -1;
+    int j0 = tx > 0 ? 1 : NX - 2, j1 = tx > 0 ? NX : -1;
+    int i0 = tz > 0 ? 1 : NZ - 2, i1 = tz > 0 ? NZ : -1;
+    for (int k = k0; k != k1; k += ty)
+      for (int j = j0; j != j1; j += tx)
+        for (int i = i0; i != i1; i += tz) {
+          long n = ((long)i * NX + j) * NY + k;
+          double t0 = tt[n];
+          sweep3_node(tt, sgn, slow, &d, i, j, k, tz > 0, tx > 0, ty > 0, tz, tx, ty, NZ, NX, NY,
+                      1);
+          if (tt[n] != t0) {
+            code[e * nn + n] = (uint8_t)((sgn[3 * n] + 1) * 9 + (sgn[3 * n + 1] + 1) * 3 +
+                                         (sgn[3 * n + 2] + 1));
+            old[e * nn + n] = t0;
+          }
+        }
+  }
+  /* seed: receivers (axes in _vinterp3d's naming: x = z axis, y = x, z = y) */
+  double gvz = 0.0;
+  for (int r = 0; r < nrec; ++r)
+    gvz += vinterp3_adjoint(ax0, NZ, ax1, NX, ax2, NY, tt, lam, rec[3 * r], rec[3 * r + 1],
+                            rec[3 * r + 2], src[0], src[1], src[2], grec[r]);
+  for (int e = nep - 1; e >= 0; --e) {
+    int tz = S[e & 7][0], tx = S[e & 7][1], ty = S[e & 7][2];
+    /* the forward loops backwards: from the last index down to the first */
+    for (int k = (ty > 0 ? NY - 1 : 0); k != (ty > 0 ? 0 : NY - 1); k -= ty)
+      for (int j = (tx > 0 ? NX - 1 : 0); j != (tx > 0 ? 0 : NX - 1); j -= tx)
+        for (int i = (tz > 0 ? NZ - 1 : 0); i != (tz > 0 ? 0 : NZ - 1); i -= tz) {
+          long n = ((long)i * NX + j) * NY + k;
+          int cd = code[e * nn + n];
+          if (cd == 255) continue;
+          double l = lam[n];
+          lam[n] = 0.0;
+          adj_push(tt, lam, gs, slow, &d, i, j, k, cd / 9 - 1, (cd / 3) % 3 - 1, cd % 3 - 1, NZ,
+                   NX, NY, l);
+          tt[n] = old[e * nn + n];
+        }
+  }
+  /* initial nodes: t = vzero * distance; vzero is the source cell's slowness */
+  {
+    double zsa = src[0] / dz, xsa = src[1] / dx, ysa = src[2] / dy;
+    zsa = zsa >= nz ? zsa - EPS : zsa;
+    xsa = xsa >= nx ? xsa - EPS : xsa;
+    ysa = ysa >= ny ? ysa - EPS : ysa;
+    int zsi = imin((int)zsa, nz - 1), xsi = imin((int)xsa, nx - 1), ysi = imin((int)ysa, ny - 1);
+    long sc = ((long)zsi * nx + xsi) * ny + ysi;
+    for (int q = 0; q < 8; ++q) {
+      int i = zsi + (q & 1), j = xsi + ((q >> 1) & 1), k = ysi + (q >> 2);
+      long n = ((long)i * NX + j) * NY + k;
+      double a = dz * (i - zsa), b = dx * (j - xsa), c = dy * (k - ysa);
+      gs[sc] += lam[n] * sqrt(a * a + b * b + c * c);
+    }
+    gs[sc] += gvz;
+  }
+done:
+  free(tt); free(tg); free(lam); free(old); free(code); free(sgn);
+  return st;
+}
+
+/* d(loss)/d(slowness) [nz][nx][ny] summed over sources; grec is
+ * [nsrc][nrec] d(loss)/d(traveltime at receiver). */
+int oracle_adjoint3d(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,
+                     const double* src, int nsrc, int nsweep, const double* rec, int nrec,
+                     const double* grec, double* grad_slow, int nthreads) {
+  long nc = (long)nz * nx * ny;
+  int NZ = nz + 1, NX = nx + 1, NY = ny + 1;
+  double* ax0 = (double*)malloc(sizeof(double) * NZ);
+  double* ax1 = (double*)malloc(sizeof(double) * NX);
+  double* ax2 = (double*)malloc(sizeof(double) * NY);
+  for (int q = 0; q < NZ; ++q) ax0[q] = dz * q;
+  for (int q = 0; q < NX; ++q) ax1[q] = dx * q;
+  for (int q = 0; q < NY; ++q) ax2[q] = dy * q;
+  double* per = (double*)calloc((size_t)nc * nsrc, sizeof(double));
+  int status = ST_OK;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) if (nthreads > 1)
+  for (int s = 0; s < nsrc; ++s) {
+    int st = adjoint3d_one(slow, nz, nx, ny, dz, dx, dy, src + 3 * s, nsweep, ax0, ax1, ax2, rec,
+                           nrec, grec + (long)s * nrec, per + (long)s * nc);
+    if (st != ST_OK) {
+#pragma omp critical
+      status = st;
+    }
+  }
+  for (long c = 0; c < nc; ++c) {
+    double g = 0.0;
+    for (int s = 0; s < nsrc; ++s) g += per[(long)s * nc + c];
+    grad_slow[c] = g;
+  }
+  free(per); free(ax0); free(ax1); free(ax2);
+  return status;
 }

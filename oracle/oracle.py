@@ -42,6 +42,10 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.oracle_fteik3d_many.argtypes = [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _I]
         L.oracle_fteik3d_many.restype = _I
+        L.oracle_fteik3d_record.argtypes = [_P, _I, _I, _I, _D, _D, _D, _D, _D, _D, _I, _P, _P, _P, _P]
+        L.oracle_fteik3d_record.restype = _I
+        L.oracle_adjoint3d.argtypes = [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _I, _P, _P, _I]
+        L.oracle_adjoint3d.restype = _I
         L.oracle_fteik2d_many.argtypes = [_P, _I, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _I]
         L.oracle_fteik2d_many.restype = _I
         L.oracle_interp3d.argtypes = [_P, _I, _P, _I, _P, _I, _P, _L, _P, _I, _D, _P]
@@ -82,6 +86,44 @@ def solve3d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
     if st == 1:
         raise ValueError("source out of bound")
     return tt, (tg if grad else None), vz
+
+
+def solve3d_record(slow, gridsize, source, nsweep=2):
+    """One 3D solve with gradients that also returns the branch record (the
+    reference's ttsgn) as int8 [nz+1, nx+1, ny+1, 3]."""
+    slow = _c(slow)
+    nz, nx, ny = slow.shape
+    tt = np.empty((nz + 1, nx + 1, ny + 1))
+    tg = np.empty((nz + 1, nx + 1, ny + 1, 3))
+    sgn = np.zeros((nz + 1, nx + 1, ny + 1, 3), dtype=np.int8)
+    vz = np.empty(1)
+    st = lib().oracle_fteik3d_record(
+        _p(slow), nz, nx, ny, *map(float, gridsize), *map(float, source), int(nsweep), _p(tt),
+        _p(tg), _p(vz), _p(sgn),
+    )
+    if st == 1:
+        raise ValueError("source out of bound")
+    return tt, tg, float(vz[0]), sgn
+
+
+def adjoint3d(slow, gridsize, sources, nsweep, receivers, grad_tt_rec, nthreads=None):
+    """d(loss)/d(slowness) [nz, nx, ny] for a loss with gradient ``grad_tt_rec``
+    [nsrc, nrec] on the apparent-velocity traveltimes at ``receivers`` (node
+    axes from the origin 0), summed over sources: the sequential reverse-mode
+    derivative of ``solve3d`` + ``vinterp``."""
+    slow = _c(slow)
+    src = _c(np.atleast_2d(sources))
+    rec = _c(np.atleast_2d(receivers))
+    g = _c(grad_tt_rec)
+    nz, nx, ny = slow.shape
+    out = np.empty_like(slow)
+    st = lib().oracle_adjoint3d(
+        _p(slow), nz, nx, ny, *map(float, gridsize), _p(src), len(src), int(nsweep), _p(rec),
+        len(rec), _p(g), _p(out), int(nthreads or os.cpu_count()),
+    )
+    if st == 1:
+        raise ValueError("source out of bound")
+    return out
 
 
 def solve2d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):

@@ -1,0 +1,107 @@
+"""The CUDA adjoint of the 3D solve (``fteik3d_solve_tape`` +
+``fteik3d_adjoint`` behind ``fteikpy_gb300.traveltimes``) against the oracle.
+
+Two references: the oracle's sequential reverse-mode adjoint (its own test
+file pins it to finite differences), compared on every cell; and central
+finite differences taken through the oracle's solve directly. The loss is
+0.5 * sum((T - T_obs)^2) over all source-receiver pairs, T the
+apparent-velocity interpolated traveltime at the receivers.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import fteikpy_gb300 as fp
+from oracle import oracle as O
+from adjoint_cases import (
+    D,
+    central_difference,
+    check_cells,
+    geometry,
+    oracle_times,
+    oracle_velocity_gradient,
+    velocity,
+)
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_gradient(v0, src, rec, nsweep, t_obs):
+    vt = torch.tensor(v0, device="cuda", requires_grad=True)
+    T = fp.traveltimes(vt, D, src, rec, nsweep)
+    loss = 0.5 * ((T - torch.as_tensor(t_obs, device="cuda")) ** 2).sum()
+    loss.backward()
+    return T.detach().cpu().numpy(), vt.grad.cpu().numpy()
+
+
+@pytest.mark.parametrize(
+    "shape,nsweep,perturb",
+    [((12, 14, 16), 1, True), ((12, 14, 16), 2, True), ((12, 14, 16), 4, True),
+     ((12, 14, 16), 2, False), ((20, 9, 33), 2, True), ((7, 40, 12), 3, False)],
+)
+def test_adjoint_equals_oracle_adjoint(shape, nsweep, perturb):
+    """Same derivative as the oracle's sequential reverse pass on every cell
+    (the sums run in another order: 1e-12 of the largest entry). The
+    perturb=False cases are pure layered models, where the slowness minima
+    tie at almost every node."""
+    src, rec = geometry(shape, 4, 30, 3)
+    t_obs = oracle_times(velocity(shape, True, perturb=perturb), src, rec, nsweep)
+    v0 = velocity(shape, False, perturb=perturb)
+    T, g = gpu_gradient(v0, src, rec, nsweep, t_obs)
+    # the forward is the reference's computation, bit for bit
+    assert np.array_equal(T, oracle_times(v0, src, rec, nsweep))
+    go = oracle_velocity_gradient(v0, src, rec, nsweep, t_obs)
+    assert np.isfinite(g).all()
+    assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()
+
+
+def test_adjoint_matches_finite_differences_through_the_oracle():
+    shape, nsweep = (12, 14, 16), 2
+    src, rec = geometry(shape, 3, 24, 1)
+    t_obs = oracle_times(velocity(shape, True), src, rec, nsweep)
+    v0 = velocity(shape, False)
+    _, g = gpu_gradient(v0, src, rec, nsweep, t_obs)
+    gmax = np.abs(g).max()
+    bad = []
+    for c in check_cells(g):
+        idx = np.unravel_index(c, shape)
+        fd = central_difference(v0, idx, 1e-6, src, rec, nsweep, t_obs)
+        if abs(fd - g[idx]) > 1e-6 * abs(fd) + 1e-10 * gmax:
+            bad.append((idx, g[idx], fd))
+    assert not bad, bad
+
+
+def test_adjoint_is_deterministic_and_batched_equals_sum():
+    shape, nsweep = (10, 12, 11), 4
+    src, rec = geometry(shape, 4, 16, 2)
+    v0 = velocity(shape, False)
+    t_obs = oracle_times(velocity(shape, True), src, rec, nsweep)
+
+    def grad(sel):
+        return gpu_gradient(v0, src[sel], rec, nsweep, t_obs[sel])[1]
+
+    g_all = grad(slice(None))
+    assert np.array_equal(g_all, grad(slice(None)))  # run to run, bit for bit
+    g_sum = sum(grad(slice(s, s + 1)) for s in range(len(src)))
+    assert np.allclose(g_all, g_sum, rtol=1e-12, atol=1e-12 * np.abs(g_all).max())
+
+
+def test_adjoint_with_zero_sweeps_and_outside_receivers():
+    """nsweep=0 leaves only the source neighbourhood; receivers outside the
+    grid contribute nothing (their traveltime is NaN and d/dT is zero)."""
+    shape = (8, 9, 10)
+    src, rec = geometry(shape, 2, 10, 4)
+    rec = np.vstack([rec, [[-5.0, 3.0, 3.0]]])
+    v0 = velocity(shape, False)
+    for nsweep in (0, 1):
+        vt = torch.tensor(v0, device="cuda", requires_grad=True)
+        T = fp.traveltimes(vt, D, src, rec, nsweep)
+        assert torch.isnan(T[:, -1]).all()
+        r = torch.nan_to_num(T, nan=0.0)
+        (0.5 * (r**2).sum()).backward()
+        g = vt.grad.cpu().numpy()
+        To = np.nan_to_num(oracle_times(v0, src, rec, nsweep))
+        s = 1.0 / v0
+        go = -O.adjoint3d(s, D, src, nsweep, rec, To) * s * s
+        assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()

@@ -386,6 +386,112 @@ def run_config2(args):
     return 0
 
 
+def uneven_models(nmodel=64, seed=44):
+    """Config-4 batch: per model, cell counts drawn uniformly from [32, 160]
+    per axis, spacing from [5, 20] m per axis, velocity 1500..2500 m/s at the
+    top plus a 0.3..1.0 1/s gradient, times (1 + 0.1 p) with p seeded normal
+    noise Gaussian-smoothed (sigma 3 cells) and rescaled to [-1, 1], and 1..16
+    seeded off-grid sources anywhere in the model."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nmodel):
+        shape = tuple(int(x) for x in rng.integers(32, 161, 3))
+        d = tuple(float(x) for x in rng.uniform(5.0, 20.0, 3))
+        z = (np.arange(shape[0]) + 0.5) * d[0]
+        v = (rng.uniform(1500.0, 2500.0) + rng.uniform(0.3, 1.0) * z)[:, None, None]
+        p = gaussian_filter(rng.standard_normal(shape), 3.0)
+        p -= p.min()
+        p = 2.0 * p / p.max() - 1.0
+        v = v * (1.0 + 0.1 * p)
+        ext = np.array(shape) * np.array(d)
+        src = rng.uniform(0.02, 0.98, (int(rng.integers(1, 17)), 3)) * ext
+        out.append((v, d, src))
+    return out
+
+
+def run_config4(args):
+    """Batched uneven models: 64 models of seeded sizes and spacings with 1-16
+    sources each, all solved (nsweep=2) by one persistent sweep launch with
+    the launch shape picked by the autotuner; beside it the same work as one
+    Eikonal3D.solve per model (64 launches) and the C oracle on a sample."""
+    import torch
+
+    import fteikpy_gb300 as fp
+    from fteikpy_gb300 import _lib
+    from oracle import oracle as O
+
+    cases = uneven_models()
+    solvers = [fp.Eikonal3D(v, d) for v, d, _ in cases]
+    sources = [s for _, _, s in cases]
+    nsrc = sum(len(s) for s in sources)
+    updates = sum(8 * NSWEEP * int(np.prod(v.shape)) * len(s) for v, _, s in cases)
+    lib = _lib.load()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, steps):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    batch = lambda: fp.solve_batch(solvers, sources, nsweep=NSWEEP)  # noqa: E731
+    lib.fteik_clear_tuning()
+    default_ms = timed(batch, max(args.steps, 1))
+    q0 = time.perf_counter()
+    shape = fp.autotune(solvers, sources)
+    tune_s = time.perf_counter() - q0
+    for _ in range(max(args.warmup - 1, 0)):
+        batch()
+    tuned_ms = timed(batch, max(args.steps, 1))
+
+    def plain():
+        return [eik.solve(src, nsweep=NSWEEP) for eik, src in zip(solvers, sources)]
+
+    plain_ms = timed(plain, max(args.steps, 1))
+    out = batch()
+    ref = plain()
+    same_as_plain = all(
+        all(np.array_equal(a.grid, b.grid) for a, b in zip(x, y)) for x, y in zip(out, ref)
+    )
+    # the C oracle on a sample of models (all host threads, parallel over sources)
+    sample = list(range(0, len(cases), 16))
+    q0 = time.perf_counter()
+    oracle_tt = [O.solve3d(1.0 / cases[m][0], cases[m][1], cases[m][2], NSWEEP, False)[0]
+                 for m in sample]
+    cpu_s = time.perf_counter() - q0
+    sample_updates = sum(8 * NSWEEP * int(np.prod(cases[m][0].shape)) * len(cases[m][2])
+                         for m in sample)
+    same_as_oracle = all(
+        np.array_equal(np.stack([t.grid for t in out[m]]), tt) for m, tt in zip(sample, oracle_tt)
+    )
+    print(json.dumps({
+        "config": 4,
+        "metric": "uneven 3D batch: 64 models (32-160 cells/axis, 5-20 m), 1-16 sources each, nsweep=2",
+        "value": 1e3 * nsrc / tuned_ms, "unit": "shots/s", "higher_is_better": True,
+        "cell_updates_per_s": updates / (tuned_ms * 1e-3),
+        "ms_per_batch": tuned_ms, "ms_per_batch_default_shape": default_ms,
+        "autotune": dict(shape, seconds=tune_s),
+        "plain_one_solve_per_model": {"ms": plain_ms, "shots_per_s": 1e3 * nsrc / plain_ms,
+                                      "launches": len(cases)},
+        "batch_over_plain": plain_ms / tuned_ms,
+        "models": len(cases), "sources": nsrc, "cell_updates": updates,
+        "bitwise_vs_per_model_solves": bool(same_as_plain),
+        "bitwise_vs_oracle_sample": bool(same_as_oracle),
+        "cpu_baseline": {"value": sample_updates / cpu_s, "unit": "cell-updates/s",
+                         "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"models {sample} with the C oracle"},
+    }))
+    return 0
+
+
 def tomography_models(shape=(96, 128, 128), d=D, seed=5):
     """Linear-gradient starting model v(z) = 1500 + 0.6 z and the true model:
     the same times (1 + 0.08 exp(-r^2 / (2 * 150 m^2))), a Gaussian anomaly of
@@ -527,9 +633,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end API timing")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-source-per-launch timing")
-    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 5],
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4, 5],
                     help="1: plain 2D solve, 2: plain 3D solve + queries + rays, 3: batched "
-                         "(default), 5: adjoint gradient")
+                         "(default), 4: uneven multi-model batch, 5: adjoint gradient")
     ap.add_argument("--fd-cells", type=int, default=50,
                     help="cells of the finite-difference check of --config 5")
     ap.add_argument("--dump", default=None,
@@ -542,12 +648,12 @@ def main():
         SHAPE, NSRC = (64, 128, 128), 32
     if args.impl == "reference":
         return run_reference(args)
-    if args.config in (1, 2, 5):
+    if args.config in (1, 2, 4, 5):
         import torch
 
         if torch.cuda.is_available():
             torch.cuda.set_device(0)
-        return {1: run_config1, 2: run_config2, 5: run_config5}[args.config](args)
+        return {1: run_config1, 2: run_config2, 4: run_config4, 5: run_config5}[args.config](args)
 
     import torch
 

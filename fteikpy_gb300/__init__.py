@@ -10,7 +10,7 @@ from .__about__ import __version__
 from ._build import build
 from ._grid import Grid2D, Grid3D, TraveltimeGrid2D, TraveltimeGrid3D
 from ._helpers import get_num_threads, set_num_threads
-from ._solver import Eikonal2D, Eikonal3D
+from ._solver import Eikonal2D, Eikonal3D, autotune, solve_batch
 from ._adjoint import converged, traveltimes
 
 __all__ = [
@@ -20,8 +20,10 @@ __all__ = [
     "Grid3D",
     "TraveltimeGrid2D",
     "TraveltimeGrid3D",
+    "autotune",
     "build",
     "converged",
+    "solve_batch",
     "traveltimes",
     "get_num_threads",
     "set_num_threads",

@@ -33,6 +33,19 @@ SIGNATURES = {
     "fteik_workspace_status": (_I, [_P, _P]),
     "fteik3d_solve_noalloc": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _LL, _P]),
     "fteik3d_adjoint_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
+    "fteik_get_option": (_I, [ctypes.c_char_p, ctypes.POINTER(_LL)]),
+    "fteik3d_batch_workspace_bytes": (_SZ, [_I, _P, _P, _I]),
+    "fteik3d_solve_batch": (
+        _I, [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P]
+    ),
+    "fteik3d_autotune": (
+        _I,
+        [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P, _P, _P],
+    ),
+    "fteik3d_batch_autotune": (
+        _I, [_I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _LL, _P, _P, _P]
+    ),
+    "fteik_clear_tuning": (_I, []),
     "fteik3d_tape_bytes": (_SZ, [_I, _I, _I, _I, _I]),
     "fteik3d_solve_tape": (
         _I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _P, _P, _SZ, _P, _SZ, _LL, _P]

@@ -25,9 +25,13 @@
 //   * their own pencil in the previous sweep, and the pencils that read it in
 //     the previous sweep (write-after-read),
 // so consecutive sweeps and all sources overlap without grid-wide barriers.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
+#include <map>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "fteik_gb300.h"
@@ -36,7 +40,6 @@
 
 namespace fteik {
 
-constexpr int kLag = kPJ + kPK - 2;
 constexpr int kWarpsPerBlock = 4;
 // Batches of at least this many sources read precomputed coefficient arrays.
 constexpr int kCoefMinSources = 4;
@@ -106,15 +109,14 @@ struct CoefCells {
 
 // One node update, _fteik3d.py:38-200, with the slowness-only factors taken
 // from the coefficient provider c (see Coef3 for which factor is which).
+// Takes the three 1D candidates (_fteik3d.py:76-104: t1d1 = tv + c.z1() ...),
+// which the caller computes first to test whether the node can change.
 template <bool GRAD, class CP>
-__device__ __forceinline__ double node_update3d(double tv, double te, double tn, double tev,
-                                                double ten, double tnv, double tnve, double t0,
+__device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
+                                                double te, double tn, double tev, double ten,
+                                                double tnv, double tnve, double t0,
                                                 const CP& c, const Ops3& o, int sz, int sx,
                                                 int sy, uint8_t& code) {
-  // 1D operators, _fteik3d.py:76-104
-  const double t1d1 = tv + c.z1();
-  const double t1d2 = te + c.x1();
-  const double t1d3 = tn + c.y1();
   const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
 
   // 2D operators, _fteik3d.py:106-143
@@ -181,25 +183,82 @@ __device__ __forceinline__ double node_update3d(double tv, double te, double tn,
   return tnew;
 }
 
+// True when the node provably keeps t0 in this sweep, on a grid with equal
+// spacings.  There every plane operator's value is its diagonal input plus a
+// non-negative root term (_fteik3d.py:113-117 with dz2i = dx2i: ta + tb =
+// 2 tev), and the 3D operator's is tnve plus one (ta + tb + tc = 3 tnve,
+// _fteik3d.py:149-158); computed in double precision each lies within
+// 2^-46 * M of that bound, M the largest input.  So if every 1D candidate is
+// >= t0 and every diagonal input is >= t0 + 2^-43 * M, no operator can beat
+// t0 (the minimum keeps t0 on ties) and the update is skipped.
+__device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, double t1d3,
+                                         double tv, double te, double tn, double tev, double ten,
+                                         double tnv, double tnve) {
+  if (!(dle(t0, t1d1) && dle(t0, t1d2) && dle(t0, t1d3))) return false;
+  // all values are >= 0, so their bit patterns order like the values
+  long long m = __double_as_longlong(t0);
+  m = max(m, __double_as_longlong(tv));
+  m = max(m, __double_as_longlong(te));
+  m = max(m, __double_as_longlong(tn));
+  m = max(m, __double_as_longlong(tev));
+  m = max(m, __double_as_longlong(ten));
+  m = max(m, __double_as_longlong(tnv));
+  m = max(m, __double_as_longlong(tnve));
+  if ((m >> 52) <= 44 || (m >> 52) >= 2047) return false;  // tiny, infinite or NaN
+  const double thr = t0 + __longlong_as_double(m - (43LL << 52));  // t0 + 2^-43 M
+  return dle(thr, tev) && dle(thr, ten) && dle(thr, tnv) && dle(thr, tnve);
+}
+
+// One model of a multi-model launch (device table built by the host).
+struct Model3 {
+  Ops3 o;
+  const double* slow;
+  Coef3 C;
+  const int* no_skip;  // this model's all-Big skip flag (see coef3d_kernel)
+  int keep_test;       // equal spacings: test keeps_t0 before the 2D/3D operators
+  int nz, nx, ny, NZ, NX, NY;
+  long long nodes;
+  int PJ, PK, T;
+  unsigned stride;
+};
+
+// One (model, source) pair of a multi-model launch.
+struct Job3 {
+  double* tt;      // this source's traveltimes
+  uint8_t* rec;    // its branch record (gradients) or null
+  unsigned* prog;  // its pencils' progress counters
+  int model, pad;
+};
+
 struct Sweep3Args {
+  // one model, nsrc sources: item t = (sweep, pencil in diagonal order, source)
   double* tt;
   uint8_t* rec;
   Coef3 C;              // precomputed coefficients (COEF variant)
   const double* slow;   // slowness cells (cell variant)
-  const int* no_skip;  // set by coef3d_kernel when the all-Big skip is not exact
+  const int* no_skip;   // set by coef3d_kernel when the all-Big skip is not exact
   uint8_t* tape_code;   // optional: per sweep, the operator code of every change
   double* tape_old;     // optional: per sweep, the value each change replaced
   unsigned* progress;
-  unsigned* ticket;
-  int* status;
   const int* order;
   int nz, nx, ny;  // cells
   int NZ, NX, NY;  // nodes
   long long nodes;
-  int nsrc, nepochs, npencils, PJ, PK, total_steps;
+  int nsrc, npencils, PJ, PK, total_steps;
   unsigned stride;
-  long long spin_limit;
+  int keep_test;  // equal spacings: test keeps_t0 before the 2D/3D operators
   Ops3 o;
+  // several models: item t = (sweep, items[t % items_per_epoch])
+  const Model3* models;
+  const Job3* jobs;
+  const int2* items;  // (job, JL << 16 | KL), by diagonal, then job
+  unsigned items_per_epoch;
+  // both
+  unsigned* ticket;
+  int* status;
+  int nepochs;
+  int chunk;  // steps between two progress publications (a power of 2)
+  long long spin_limit;
 };
 
 // Lane-0 bounded wait until *p >= target.  Gives up (and flags the status)
@@ -218,33 +277,83 @@ __device__ __forceinline__ bool wait_geq(const unsigned* p, unsigned target, int
   }
 }
 
-template <bool GRAD, bool COEF>
+// The persistent sweep kernel.  PW is the pencil width along j (the pencil is
+// PW x 32/PW columns); MULTI takes items from the multi-model tables.
+template <bool GRAD, bool COEF, int PW, bool MULTI>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
-    sweep3d_kernel(const Sweep3Args A) {
+    sweep3d_kernel(const __grid_constant__ Sweep3Args A) {
+  constexpr int PJW = PW, PKW = 32 / PW, LAG = PJW + PKW - 2;
   const int lane = threadIdx.x & 31;
-  const int lj = lane >> 3, lk = lane & 7;
-  const Ops3& o = A.o;
-  const long long NXY = (long long)A.NX * A.NY;
-  const unsigned total_items = (unsigned)A.nepochs * A.npencils * A.nsrc;
-  const int T = A.total_steps;
+  const int lj = lane / PKW, lk = lane % PKW;
+  const unsigned per_epoch = MULTI ? A.items_per_epoch : (unsigned)A.npencils * A.nsrc;
+  const unsigned total_items = (unsigned)A.nepochs * per_epoch;
+  const unsigned cmask = (unsigned)A.chunk - 1u;
 
   for (;;) {
     unsigned t = 0;
     if (lane == 0) t = atomicAdd(A.ticket, 1u);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= total_items) break;
-    const int e = (int)(t / ((unsigned)A.npencils * A.nsrc));
-    const unsigned rem = t - (unsigned)e * A.npencils * A.nsrc;
-    const int p = (int)(rem / A.nsrc);
-    const int src = (int)(rem - (unsigned)p * A.nsrc);
+    const int e = (int)(t / per_epoch);
+    const unsigned rem = t - (unsigned)e * per_epoch;
+    // Geometry of this item's model and source.
+    const Ops3* op;
+    const double* slow;
+    const int* no_skip;
+    Coef3 C;
+    double* tts;
+    uint8_t* recs;
+    unsigned* prog;
+    int nx, ny, NZ, NX, NY, PJ, PK, T, JL, KL, src, keep_test;
+    long long nodes;
+    unsigned stride;
+    if constexpr (MULTI) {
+      const int2 it = A.items[rem];
+      const Job3 jb = A.jobs[it.x];
+      const Model3& M = A.models[jb.model];
+      op = &M.o;
+      slow = M.slow;
+      no_skip = M.no_skip;
+      if (COEF) C = M.C;
+      tts = jb.tt;
+      recs = jb.rec;
+      prog = jb.prog;
+      nx = M.nx; ny = M.ny;
+      NZ = M.NZ; NX = M.NX; NY = M.NY;
+      PJ = M.PJ; PK = M.PK; T = M.T;
+      nodes = M.nodes;
+      stride = M.stride;
+      keep_test = M.keep_test;
+      JL = it.y >> 16;
+      KL = it.y & 0xffff;
+      src = it.x;
+    } else {
+      const int p = (int)(rem / A.nsrc);
+      src = (int)(rem - (unsigned)p * A.nsrc);
+      op = &A.o;
+      slow = A.slow;
+      no_skip = A.no_skip;
+      if (COEF) C = A.C;
+      tts = A.tt + (long long)src * A.nodes;
+      recs = GRAD ? A.rec + (long long)src * A.nodes : nullptr;
+      prog = A.progress + (long long)src * A.npencils;
+      nx = A.nx; ny = A.ny;
+      NZ = A.NZ; NX = A.NX; NY = A.NY;
+      PJ = A.PJ; PK = A.PK; T = A.total_steps;
+      nodes = A.nodes;
+      stride = A.stride;
+      keep_test = A.keep_test;
+      JL = A.order[p] >> 16;
+      KL = A.order[p] & 0xffff;
+    }
+    const Ops3& o = *op;
+    const long long NXY = (long long)NX * NY;
     const int dir = e & 7;
     const int sz = dir < 4 ? 1 : -1, sx = (dir & 1) ? -1 : 1, sy = (dir & 2) ? -1 : 1;
-    const int JL = A.order[p] >> 16, KL = A.order[p] & 0xffff;
-    const int J = sx > 0 ? JL : A.PJ - 1 - JL;
-    const int K = sy > 0 ? KL : A.PK - 1 - KL;
-    unsigned* prog = A.progress + (long long)src * A.npencils;
-    unsigned* my_prog = prog + J * A.PK + K;
-    const unsigned base = (unsigned)e * A.stride;
+    const int J = sx > 0 ? JL : PJ - 1 - JL;
+    const int K = sy > 0 ? KL : PK - 1 - KL;
+    unsigned* my_prog = prog + J * PK + K;
+    const unsigned base = (unsigned)e * stride;
 
     // Dependencies on the previous sweep: this pencil, and the pencils that
     // read it (its downwind neighbours in the previous direction).
@@ -252,13 +361,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     if (lane == 0 && e > 0) {
       const int pd = (e - 1) & 7;
       const int psx = (pd & 1) ? -1 : 1, psy = (pd & 2) ? -1 : 1;
-      const unsigned done = base - A.stride + (unsigned)T;
+      const unsigned done = base - stride + (unsigned)T;
       ok = wait_geq(my_prog, done, A.status, A.spin_limit);
       const int J2 = J + psx, K2 = K + psy;
-      const bool hj = J2 >= 0 && J2 < A.PJ, hk = K2 >= 0 && K2 < A.PK;
-      if (ok && hj) ok = wait_geq(prog + J2 * A.PK + K, done, A.status, A.spin_limit);
-      if (ok && hk) ok = wait_geq(prog + J * A.PK + K2, done, A.status, A.spin_limit);
-      if (ok && hj && hk) ok = wait_geq(prog + J2 * A.PK + K2, done, A.status, A.spin_limit);
+      const bool hj = J2 >= 0 && J2 < PJ, hk = K2 >= 0 && K2 < PK;
+      if (ok && hj) ok = wait_geq(prog + J2 * PK + K, done, A.status, A.spin_limit);
+      if (ok && hk) ok = wait_geq(prog + J * PK + K2, done, A.status, A.spin_limit);
+      if (ok && hj && hk) ok = wait_geq(prog + J2 * PK + K2, done, A.status, A.spin_limit);
     }
     ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     if (!ok) {
@@ -269,47 +378,44 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 
     // Upwind pencils of this sweep.
     const int Ju = J - sx, Ku = K - sy;
-    const bool hJu = Ju >= 0 && Ju < A.PJ, hKu = Ku >= 0 && Ku < A.PK;
-    const unsigned* prog_j = prog + Ju * A.PK + K;
-    const unsigned* prog_k = prog + J * A.PK + Ku;
-    const unsigned* prog_jk = prog + Ju * A.PK + Ku;
+    const bool hJu = Ju >= 0 && Ju < PJ, hKu = Ku >= 0 && Ku < PK;
+    const unsigned* prog_j = prog + Ju * PK + K;
+    const unsigned* prog_k = prog + J * PK + Ku;
+    const unsigned* prog_jk = prog + Ju * PK + Ku;
 
-    const int j = sx > 0 ? J * kPJ + lj : J * kPJ + (kPJ - 1) - lj;
-    const int k = sy > 0 ? K * kPK + lk : K * kPK + (kPK - 1) - lk;
-    const bool in_grid = j < A.NX && k < A.NY;
-    const bool frozen_jk = (j == (sx > 0 ? 0 : A.NX - 1)) || (k == (sy > 0 ? 0 : A.NY - 1));
+    const int j = sx > 0 ? J * PJW + lj : J * PJW + (PJW - 1) - lj;
+    const int k = sy > 0 ? K * PKW + lk : K * PKW + (PKW - 1) - lk;
+    const bool in_grid = j < NX && k < NY;
+    const bool frozen_jk = (j == (sx > 0 ? 0 : NX - 1)) || (k == (sy > 0 ? 0 : NY - 1));
     // Offsets of the coefficient reads that depend on the column only (see
     // Coef3): j1, k1 are the upwind cell indices of the reference.
     const int j1 = sx > 0 ? j - 1 : j, k1 = sy > 0 ? k - 1 : k;
-    const long long jk = (long long)j * A.NY + k;
-    const long long j1k = (long long)j1 * A.NY + k, jk1 = (long long)j * A.NY + k1;
-    const long long j1k1 = (long long)j1 * A.NY + k1;
+    const long long jk = (long long)j * NY + k;
+    const long long j1k = (long long)j1 * NY + k, jk1 = (long long)j * NY + k1;
+    const long long j1k1 = (long long)j1 * NY + k1;
     // Slowness cell offsets around the column, upwind cell first (CoefCells).
-    const int jm = imax(j - 1, 0), jp = imin(j, A.NX - 2);
-    const int km = imax(k - 1, 0), kp = imin(k, A.NY - 2);
-    const long long NYc = A.ny, NXYc = (long long)A.nx * A.ny;
+    const int jm = imax(j - 1, 0), jp = imin(j, NX - 2);
+    const int km = imax(k - 1, 0), kp = imin(k, NY - 2);
+    const long long NYc = ny, NXYc = (long long)nx * ny;
     const long long ju = (sx > 0 ? jm : jp) * NYc, jo = (sx > 0 ? jp : jm) * NYc;
     const long long ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
-    double* tts = A.tt + (long long)src * A.nodes;
-    uint8_t* recs = GRAD ? A.rec + (long long)src * A.nodes : nullptr;
-    const long long dj = (long long)sx * A.NY, dk = sy;
+    const long long dj = (long long)sx * NY, dk = sy;
     const long long di = (long long)sz * NXY;
-    const bool may_skip = *A.no_skip == 0;
+    const bool may_skip = *no_skip == 0;
     const long long big_bits = __double_as_longlong(kBig);
 
     double r1 = 0.0, r2 = 0.0, r3 = 0.0;
-    constexpr int kChunk = 4;
     for (int s = 0; s < T; ++s) {
-      if ((s % kChunk) == 0) {
-        // Upwind data needed by the steps s .. s+kChunk-1 of this chunk.
-        const int last = imin(s + kChunk - 1, T - 1);
+      if (((unsigned)s & cmask) == 0) {
+        // Upwind data needed by the steps s .. s+chunk-1 of this chunk.
+        const int last = imin(s + (int)cmask, T - 1);
         bool w = true;
         if (lane == 0) {
-          if (hJu) w = wait_geq(prog_j, base + (unsigned)imin(last + kPJ, T), A.status, A.spin_limit);
+          if (hJu) w = wait_geq(prog_j, base + (unsigned)imin(last + PJW, T), A.status, A.spin_limit);
           if (w && hKu)
-            w = wait_geq(prog_k, base + (unsigned)imin(last + kPK, T), A.status, A.spin_limit);
+            w = wait_geq(prog_k, base + (unsigned)imin(last + PKW, T), A.status, A.spin_limit);
           if (w && hJu && hKu)
-            w = wait_geq(prog_jk, base + (unsigned)imin(last + kLag + 1, T), A.status,
+            w = wait_geq(prog_jk, base + (unsigned)imin(last + LAG + 1, T), A.status,
                          A.spin_limit);
           if (w) __threadfence();
         }
@@ -317,15 +423,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         __syncwarp();
         if (!w) break;
       }
-      const double u8_1 = __shfl_up_sync(0xffffffffu, r1, 8);
-      const double u8_2 = __shfl_up_sync(0xffffffffu, r2, 8);
-      const double u1_1 = __shfl_up_sync(0xffffffffu, r1, 1);
-      const double u1_2 = __shfl_up_sync(0xffffffffu, r2, 1);
-      const double u9_2 = __shfl_up_sync(0xffffffffu, r2, 9);
-      const double u9_3 = __shfl_up_sync(0xffffffffu, r3, 9);
+      const double uj_1 = __shfl_up_sync(0xffffffffu, r1, PKW);
+      const double uj_2 = __shfl_up_sync(0xffffffffu, r2, PKW);
+      const double uk_1 = __shfl_up_sync(0xffffffffu, r1, 1);
+      const double uk_2 = __shfl_up_sync(0xffffffffu, r2, 1);
+      const double ujk_2 = __shfl_up_sync(0xffffffffu, r2, PKW + 1);
+      const double ujk_3 = __shfl_up_sync(0xffffffffu, r3, PKW + 1);
       const int r = s - lj - lk;
-      const bool act = in_grid && r >= 0 && r < A.NZ;
-      const int i = sz > 0 ? r : A.NZ - 1 - r;
+      const bool act = in_grid && r >= 0 && r < NZ;
+      const int i = sz > 0 ? r : NZ - 1 - r;
       const long long n = (long long)i * NXY + jk;
       const double t0 = act ? ld_cg(tts + n) : 0.0;
       double res = t0;
@@ -333,12 +439,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       double tv = 0.0, te = 0.0, tn = 0.0, tev = 0.0, tnv = 0.0, ten = 0.0, tnve = 0.0;
       if (upd) {
         tv = r1;
-        te = lj > 0 ? u8_1 : ld_cg(tts + n - dj);
-        tn = lk > 0 ? u1_1 : ld_cg(tts + n - dk);
-        tev = lj > 0 ? u8_2 : ld_cg(tts + n - di - dj);
-        tnv = lk > 0 ? u1_2 : ld_cg(tts + n - di - dk);
-        ten = (lj > 0 && lk > 0) ? u9_2 : ld_cg(tts + n - dj - dk);
-        tnve = (lj > 0 && lk > 0) ? u9_3 : ld_cg(tts + n - di - dj - dk);
+        te = lj > 0 ? uj_1 : ld_cg(tts + n - dj);
+        tn = lk > 0 ? uk_1 : ld_cg(tts + n - dk);
+        tev = lj > 0 ? uj_2 : ld_cg(tts + n - di - dj);
+        tnv = lk > 0 ? uk_2 : ld_cg(tts + n - di - dk);
+        ten = (lj > 0 && lk > 0) ? ujk_2 : ld_cg(tts + n - dj - dk);
+        tnve = (lj > 0 && lk > 0) ? ujk_3 : ld_cg(tts + n - di - dj - dk);
         // A node whose value and 7 upwind neighbours all still hold Big keeps
         // Big (every operator then returns at least Big; coef3d_kernel checks
         // the scale condition that makes this exact).
@@ -352,34 +458,48 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         }
       }
       if (__any_sync(0xffffffffu, upd)) {
+        // Coefficients (see Coef3): read lazily from the arrays, or derived
+        // from the 8 slowness cells around the node.
+        const long long i0 = (long long)i * NXY;
+        const long long i1 = (long long)(sz > 0 ? i - 1 : i) * NXY;
+        const CoefArrays ca{C,        i1 + jk,  i0 + j1k,  i0 + jk1,
+                            i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
+        CoefCells cc{{}, o};
+        double t1d1 = 0.0, t1d2 = 0.0, t1d3 = 0.0;
+        bool go = upd;
         if (upd) {
-          uint8_t code = 0;
           if (COEF) {
-            const long long i0 = (long long)i * NXY;
-            const long long i1 = (long long)(sz > 0 ? i - 1 : i) * NXY;
-            const CoefArrays cp{A.C,      i1 + jk,   i0 + j1k,   i0 + jk1,
-                                i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
-            res = node_update3d<GRAD>(tv, te, tn, tev, ten, tnv, tnve, t0, cp, o, sz, sx, sy,
-                                      code);
+            t1d1 = tv + ca.z1();
+            t1d2 = te + ca.x1();
+            t1d3 = tn + ca.y1();
           } else {
-            const int im = imax(i - 1, 0), ip = imin(i, A.NZ - 2);
+            const int im = imax(i - 1, 0), ip = imin(i, NZ - 2);
             const long long iu = (sz > 0 ? im : ip) * NXYc, io = (sz > 0 ? ip : im) * NXYc;
-            CoefCells cp{{}, o};
 #pragma unroll
             for (int a = 0; a < 2; ++a)
 #pragma unroll
               for (int b = 0; b < 2; ++b)
 #pragma unroll
                 for (int c = 0; c < 2; ++c)
-                  cp.U[a][b][c] = __ldg(A.slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
-            res = node_update3d<GRAD>(tv, te, tn, tev, ten, tnv, tnve, t0, cp, o, sz, sx, sy,
-                                      code);
+                  cc.U[a][b][c] = __ldg(slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
+            t1d1 = tv + cc.z1();
+            t1d2 = te + cc.x1();
+            t1d3 = tn + cc.y1();
           }
+          if (keep_test)
+            go = !keeps_t0(t0, t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve);
+        }
+        if (__any_sync(0xffffffffu, go) && go) {
+          uint8_t code = 0;
+          res = COEF ? node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
+                                           ca, o, sz, sx, sy, code)
+                     : node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
+                                           cc, o, sz, sx, sy, code);
           if (!deq(res, t0)) {
             tts[n] = res;
             if (GRAD) recs[n] = code;
-            if (A.tape_code) {
-              const long long tq = ((long long)e * A.nsrc + src) * A.nodes + n;
+            if (!MULTI && A.tape_code) {
+              const long long tq = ((long long)e * A.nsrc + src) * nodes + n;
               A.tape_code[tq] = code;
               A.tape_old[tq] = t0;
             }
@@ -389,7 +509,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       r3 = r2;
       r2 = r1;
       r1 = res;
-      if (((s + 1) % kChunk) == 0 || s + 1 == T) {
+      if (((unsigned)(s + 1) & cmask) == 0 || s + 1 == T) {
         __syncwarp();
         if (lane == 0) {
           __threadfence();
@@ -420,13 +540,12 @@ __global__ void fill3d_kernel(double* tt, uint8_t* rec, long long n) {
 // neighbourhood provably stays Big (every operator exceeds Big by at least
 // about slowness * spacing / 2, far above the rounding of Big), which makes
 // the sweep's skip of such nodes exact; otherwise the skip is disabled.
-__global__ void coef3d_kernel(const double* slow, int nz, int nx, int ny, Ops3 o, Coef3 C,
-                              bool write, int* no_skip) {
-  const int NX = nx + 1, NY = ny + 1;
-  const long long n_nodes = (long long)(nz + 1) * NX * NY;
-  const double hmin = fmin(o.dz, fmin(o.dx, o.dy));
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_nodes;
-       q += (long long)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void coef3d_node(long long q, const double* slow, int nz, int nx,
+                                            int ny, const Ops3& o, const Coef3& C, bool write,
+                                            int* no_skip) {
+  {
+    const int NX = nx + 1, NY = ny + 1;
+    const double hmin = fmin(o.dz, fmin(o.dx, o.dy));
     const int i = (int)(q / ((long long)NX * NY));
     const int j = (int)((q / NY) % NX);
     const int k = (int)(q % NY);
@@ -437,7 +556,7 @@ __global__ void coef3d_kernel(const double* slow, int nz, int nx, int ny, Ops3 o
     double v;
     if (!write) {
       if (i < nz && j < nx && k < ny && !(S(i, j, k) * hmin >= 1e-9)) atomicOr(no_skip, 1);
-      continue;
+      return;
     }
     if (i < nz) {
       v = pmin(pmin(S(i, jm, km), S(i, jm, kp)), pmin(S(i, jp, km), S(i, jp, kp)));
@@ -478,14 +597,27 @@ __global__ void coef3d_kernel(const double* slow, int nz, int nx, int ny, Ops3 o
   }
 }
 
-// Source set-up, _fteik3d.py:409-456: one thread per source.
-__global__ void init3d_kernel(const double* slow, const double* src, int nsrc, int nz, int nx,
-                              int ny, Ops3 o, double* tt, long long nodes, Source3* params,
-                              double* vzero_out) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsrc) return;
+__global__ void coef3d_kernel(const double* slow, int nz, int nx, int ny, Ops3 o, Coef3 C,
+                              bool write, int* no_skip) {
+  const long long n_nodes = (long long)(nz + 1) * (nx + 1) * (ny + 1);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n_nodes;
+       q += (long long)gridDim.x * blockDim.x)
+    coef3d_node(q, slow, nz, nx, ny, o, C, write, no_skip);
+}
+
+// The same for every model of a batch: blockIdx.y = model.
+__global__ void coef3d_batch_kernel(const Model3* models, bool write) {
+  const Model3& M = models[blockIdx.y];
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < M.nodes;
+       q += (long long)gridDim.x * blockDim.x)
+    coef3d_node(q, M.slow, M.nz, M.nx, M.ny, M.o, M.C, write, (int*)M.no_skip);
+}
+
+// Source set-up, _fteik3d.py:409-456.
+__device__ __forceinline__ Source3 init3d_source(const double* slow, const double* src, int nz,
+                                                 int nx, int ny, const Ops3& o, double* t) {
   Source3 p;
-  double zsa = src[3 * s] / o.dz, xsa = src[3 * s + 1] / o.dx, ysa = src[3 * s + 2] / o.dy;
+  double zsa = src[0] / o.dz, xsa = src[1] / o.dx, ysa = src[2] / o.dy;
   zsa = zsa >= nz ? zsa - kEps : zsa;
   xsa = xsa >= nx ? xsa - kEps : xsa;
   ysa = ysa >= ny ? ysa - kEps : ysa;
@@ -497,52 +629,103 @@ __global__ void init3d_kernel(const double* slow, const double* src, int nsrc, i
   p.ysi = imin((int)ysa, ny - 1);
   p.pad = 0;
   p.vzero = slow[((long long)p.zsi * nx + p.xsi) * ny + p.ysi];
-  params[s] = p;
-  vzero_out[s] = p.vzero;
   const int NX = nx + 1, NY = ny + 1;
-  double* t = tt + (long long)s * nodes;
   for (int q = 0; q < 8; ++q) {
     const int i = p.zsi + (q & 1), j = p.xsi + ((q >> 1) & 1), k = p.ysi + ((q >> 2) & 1);
     double tzc, txc, tyc;
     t[((long long)i * NX + j) * NY + k] = t_anad3(i, j, k, o, p, tzc, txc, tyc);
+  }
+  return p;
+}
+
+// One thread per source.
+__global__ void init3d_kernel(const double* slow, const double* src, int nsrc, int nz, int nx,
+                              int ny, Ops3 o, double* tt, long long nodes, Source3* params,
+                              double* vzero_out) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsrc) return;
+  const Source3 p = init3d_source(slow, src + 3 * s, nz, nx, ny, o, tt + (long long)s * nodes);
+  params[s] = p;
+  vzero_out[s] = p.vzero;
+}
+
+// One thread per job (model, source) of a batch.
+__global__ void init3d_batch_kernel(const Model3* models, const Job3* jobs, int njobs,
+                                    const double* src, Source3* params, double* vzero_out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= njobs) return;
+  const Job3 jb = jobs[q];
+  const Model3& M = models[jb.model];
+  const Source3 p = init3d_source(M.slow, src + 3 * q, M.nz, M.nx, M.ny, M.o, jb.tt);
+  params[q] = p;
+  vzero_out[q] = p.vzero;
+}
+
+// Fill every node of every job with Big (and its record with "no sign"):
+// blockIdx.y = job.
+__global__ void fill3d_batch_kernel(const Model3* models, const Job3* jobs) {
+  const Job3 jb = jobs[blockIdx.y];
+  const long long n = models[jb.model].nodes;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    jb.tt[q] = kBig;
+    if (jb.rec) jb.rec[q] = 13;
   }
 }
 
 // Gradient post-pass, _fteik3d.py:464-488.  The 8 nodes around the source
 // start from the analytic derivatives they were initialised with
 // (_fteik3d.py:453-456); every other node starts from zero.
+__device__ __forceinline__ void grad3d_node(const double* tt, const uint8_t* rec, long long n,
+                                            const Source3& p, int NX, int NY, const Ops3& o,
+                                            double* g) {
+  const long long NXY = (long long)NX * NY;
+  const int i = (int)(n / NXY);
+  const int j = (int)((n - (long long)i * NXY) / NY);
+  const int k = (int)(n - (long long)i * NXY - (long long)j * NY);
+  double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+  if ((unsigned)(i - p.zsi) <= 1u && (unsigned)(j - p.xsi) <= 1u && (unsigned)(k - p.ysi) <= 1u)
+    t_anad3(i, j, k, o, p, g0, g1, g2);
+  const int code = rec[n];
+  const int cz = code / 9 - 1, cx = (code / 3) % 3 - 1, cy = code % 3 - 1;
+  const double tq = tt[n];
+  if (cz != 0) g0 = div_by((double)cz * (tq - tt[n - cz * NXY]), o.rdz);
+  if (cx != 0) g1 = div_by((double)cx * (tq - tt[n - (long long)cx * NY]), o.rdx);
+  if (cy != 0) g2 = div_by((double)cy * (tq - tt[n - cy]), o.rdy);
+  const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+  if (gn > 0.0) {
+    g0 /= gn;
+    g1 /= gn;
+    g2 /= gn;
+  }
+  g[3 * n] = g0;
+  g[3 * n + 1] = g1;
+  g[3 * n + 2] = g2;
+}
+
 __global__ void grad3d_kernel(const double* tt, const uint8_t* rec, const Source3* params,
                               int nsrc, int NZ, int NX, int NY, Ops3 o, double* ttgrad) {
   const long long nodes = (long long)NZ * NX * NY;
   const long long total = nodes * nsrc;
-  const long long NXY = (long long)NX * NY;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
     const int s = (int)(q / nodes);
-    const long long n = q - (long long)s * nodes;
-    const int i = (int)(n / NXY);
-    const int j = (int)((n - (long long)i * NXY) / NY);
-    const int k = (int)(n - (long long)i * NXY - (long long)j * NY);
-    const Source3 p = params[s];
-    double g0 = 0.0, g1 = 0.0, g2 = 0.0;
-    if ((unsigned)(i - p.zsi) <= 1u && (unsigned)(j - p.xsi) <= 1u && (unsigned)(k - p.ysi) <= 1u)
-      t_anad3(i, j, k, o, p, g0, g1, g2);
-    const int code = rec[q];
-    const int cz = code / 9 - 1, cx = (code / 3) % 3 - 1, cy = code % 3 - 1;
-    const double tq = tt[q];
-    if (cz != 0) g0 = div_by((double)cz * (tq - tt[q - cz * NXY]), o.rdz);
-    if (cx != 0) g1 = div_by((double)cx * (tq - tt[q - (long long)cx * NY]), o.rdx);
-    if (cy != 0) g2 = div_by((double)cy * (tq - tt[q - cy]), o.rdy);
-    const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
-    if (gn > 0.0) {
-      g0 /= gn;
-      g1 /= gn;
-      g2 /= gn;
-    }
-    ttgrad[3 * q] = g0;
-    ttgrad[3 * q + 1] = g1;
-    ttgrad[3 * q + 2] = g2;
+    const long long off = (long long)s * nodes;
+    grad3d_node(tt + off, rec + off, q - off, params[s], NX, NY, o, ttgrad + 3 * off);
   }
+}
+
+// Gradients of every job of a batch: blockIdx.y = job; grads[job] is where
+// that source's [nodes][3] gradients go.
+__global__ void grad3d_batch_kernel(const Model3* models, const Job3* jobs,
+                                    const Source3* params, double* const* grads) {
+  const Job3 jb = jobs[blockIdx.y];
+  const Model3& M = models[jb.model];
+  const Source3 p = params[blockIdx.y];
+  double* g = grads[blockIdx.y];
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < M.nodes;
+       q += (long long)gridDim.x * blockDim.x)
+    grad3d_node(jb.tt, jb.rec, q, p, M.NX, M.NY, M.o, g);
 }
 
 // Work order of the pencils inside one sweep: by diagonal JL + KL (in the
@@ -560,6 +743,86 @@ __global__ void pencil_order_kernel(int PJ, int PK, int* order) {
 
 // ---------------------------------------------------------------- host side --
 
+// Launch shape of the sweep kernel: pencil width (2, 4, 8), steps between
+// progress publications (power of 2), coefficient source (1 arrays, 0 cells).
+struct Tune3 {
+  int pencil, chunk, coef;
+};
+
+static const void* sweep_kernel(int grad, bool coef, int pencil, bool multi) {
+#define FTEIK_K(G, C, P, M) (const void*)sweep3d_kernel<G, C, P, M>
+#define FTEIK_KP(G, C, M) \
+  (pencil == 2 ? FTEIK_K(G, C, 2, M) : pencil == 8 ? FTEIK_K(G, C, 8, M) : FTEIK_K(G, C, 4, M))
+  const bool g = grad != 0;  // 1: gradients, 2: branch record for the tape
+  if (multi) {
+    if (g) return coef ? FTEIK_KP(true, true, true) : FTEIK_KP(true, false, true);
+    return coef ? FTEIK_KP(false, true, true) : FTEIK_KP(false, false, true);
+  }
+  if (g) return coef ? FTEIK_KP(true, true, false) : FTEIK_KP(true, false, false);
+  return coef ? FTEIK_KP(false, true, false) : FTEIK_KP(false, false, false);
+#undef FTEIK_KP
+#undef FTEIK_K
+}
+
+// Launch shapes measured by the autotuner, per problem signature.
+static std::mutex g_tune_mu;
+static std::map<std::vector<long long>, Tune3> g_tuned;
+
+static bool tuned_lookup(const std::vector<long long>& key, Tune3* t) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tuned.find(key);
+  if (it == g_tuned.end()) return false;
+  *t = it->second;
+  return true;
+}
+
+static void tuned_store(const std::vector<long long>& key, const Tune3& t) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned[key] = t;
+}
+
+// The shape a solve runs with: explicit options first, then a shape the
+// autotuner measured for this signature, then the defaults (coefficient
+// arrays once `coef_sources` sources share them).
+static Tune3 resolve_tune(const std::vector<long long>& key, int coef_sources) {
+  Tune3 t{kDefaultPencil, kDefaultChunk, coef_sources >= kCoefMinSources ? 1 : 0};
+  Tune3 m;
+  if (tuned_lookup(key, &m)) t = m;
+  const long long op = option_value(kOptSweepPencil), oc = option_value(kOptSweepChunk),
+                  of = option_value(kOptSweepCoef);
+  if (op > 0) t.pencil = (int)op;
+  if (oc > 0) t.chunk = (int)oc;
+  if (of >= 0) t.coef = (int)of;
+  return t;
+}
+
+static std::vector<long long> single_key(int nz, int nx, int ny, int nsrc, int grad) {
+  return {0, nz, nx, ny, nsrc, grad == 1};
+}
+
+// Persistent launch of the sweep kernel over `items` work items.
+static int launch_sweep(const void* kern, const Sweep3Args& A, long long items, cudaStream_t st) {
+  int blocks = resident_blocks(kern, kWarpsPerBlock * 32);
+  const long long need = (items + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  if (need < blocks) blocks = (int)need;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  timing_events(&ev0, &ev1);
+  if (ev0) FTEIK_CHECK(cudaEventRecord(ev0, st));
+  void* args[] = {(void*)&A};
+  FTEIK_CHECK(cudaLaunchKernel(kern, dim3(blocks), dim3(kWarpsPerBlock * 32), args, 0, st));
+  if (ev1) FTEIK_CHECK(cudaEventRecord(ev1, st));
+  return kOk;
+}
+
+// The unchanged-node test (keeps_t0) holds for equal spacings; the option
+// "sweep_keep_test" = 0 turns it off.
+static int keep_test_enabled(double dz, double dx, double dy) {
+  return dz == dx && dx == dy && option_value(kOptKeepTest) != 0 ? 1 : 0;
+}
+
+static void sweep_args_defaults(Sweep3Args& A) {
+  std::memset((void*)&A, 0, sizeof(A));
+}
 
 }  // namespace fteik
 
@@ -574,7 +837,7 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
                         double dy, const double* sources, int nsrc, int nsweep, int grad,
                         double* tt, double* ttgrad, double* vzero, void* workspace,
                         size_t workspace_bytes, uint8_t* tape_code, double* tape_old,
-                        long long spin_limit, void* stream) {
+                        long long spin_limit, void* stream, const Tune3* force = nullptr) {
   cudaStream_t st = (cudaStream_t)stream;
   if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || nsweep < 0 || !slow || !sources || !tt ||
       !vzero || !workspace || grad < 0 || grad > 2 || (grad == 1 && !ttgrad))
@@ -590,10 +853,12 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
                     (0.0 <= y && y <= dy * ny);
     if (!ok) return kSourceOutOfBound;
   }
+  const Tune3 tune = force ? *force : resolve_tune(single_key(nz, nx, ny, nsrc, grad), nsrc);
+  const int pw = tune.pencil, pk = 32 / pw;
   const int NZ = nz + 1, NX = nx + 1, NY = ny + 1;
-  const int PJ = (NX + kPJ - 1) / kPJ, PK = (NY + kPK - 1) / kPK;
+  const int PJ = (NX + pw - 1) / pw, PK = (NY + pk - 1) / pk;
   const long long nodes = (long long)NZ * NX * NY;
-  const int T = NZ + kLag;
+  const int T = NZ + pw + pk - 2;
   const unsigned long long stride = (unsigned long long)T + 1;
   const unsigned long long nepochs = 8ull * nsweep;
   if (nepochs * stride >= (1ull << 31) || nepochs * PJ * PK * (unsigned long long)nsrc >= (1ull << 31) ||
@@ -625,8 +890,7 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
   pencil_order_kernel<<<(PJ * PK + 127) / 128, 128, 0, st>>>(PJ, PK, order);
   // Coefficient arrays pay off when enough sources share them (they stay in
   // L2 across the sources of a pencil); a few sources read the slowness cells.
-  const long long opt_coef = option_value(kOptSweepCoef);
-  const bool use_coef = opt_coef < 0 ? nsrc >= kCoefMinSources : opt_coef != 0;
+  const bool use_coef = tune.coef != 0;
   coef3d_kernel<<<grid_for(nodes, 256), 256, 0, st>>>(slow, nz, nx, ny, o, C, use_coef, no_skip);
   const long long ntot = nodes * nsrc;
   fill3d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
@@ -635,6 +899,7 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
   FTEIK_CHECK(cudaGetLastError());
   if (nsweep > 0) {
     Sweep3Args A;
+    sweep_args_defaults(A);
     A.tt = tt;
     A.rec = rec;
     A.C = C;
@@ -660,22 +925,13 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
     A.PK = PK;
     A.total_steps = T;
     A.stride = (unsigned)stride;
+    A.chunk = tune.chunk;
     A.spin_limit = spin_limit > 0 ? spin_limit : (1LL << 25);
+    A.keep_test = keep_test_enabled(dz, dx, dy);
     A.o = o;
     const long long items = (long long)nepochs * PJ * PK * nsrc;
-    const void* kern = grad ? (use_coef ? (const void*)sweep3d_kernel<true, true>
-                                        : (const void*)sweep3d_kernel<true, false>)
-                            : (use_coef ? (const void*)sweep3d_kernel<false, true>
-                                        : (const void*)sweep3d_kernel<false, false>);
-    int blocks = resident_blocks(kern, kWarpsPerBlock * 32);
-    const long long need = (items + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    if (need < blocks) blocks = (int)need;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    timing_events(&ev0, &ev1);
-    if (ev0) FTEIK_CHECK(cudaEventRecord(ev0, st));
-    void* args[] = {(void*)&A};
-    FTEIK_CHECK(cudaLaunchKernel(kern, dim3(blocks), dim3(kWarpsPerBlock * 32), args, 0, st));
-    if (ev1) FTEIK_CHECK(cudaEventRecord(ev1, st));
+    const int rc = launch_sweep(sweep_kernel(grad, use_coef, pw, false), A, items, st);
+    if (rc != kOk) return rc;
   }
   if (grad == 1) {
     grad3d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, params, nsrc, NZ, NX, NY, o,
@@ -712,7 +968,7 @@ extern "C" int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, do
   uint8_t* code = (uint8_t*)tape;
   double* old = (double*)((char*)tape + align_up(n));
   // 255 marks "unchanged in this sweep"
-  FTEIK_CHECK(cudaMemsetAsync(code, 0xff, n, (cudaStream_t)stream));
+  if (n) FTEIK_CHECK(cudaMemsetAsync(code, 0xff, n, (cudaStream_t)stream));
   int rc = solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, nsweep, 2, tt, nullptr,
                         vzero, workspace, workspace_bytes, code, old, spin_limit, stream);
   if (rc != kOk) return rc;
@@ -727,4 +983,376 @@ extern "C" int fteik3d_solve(const double* slow, int nz, int nx, int ny, double 
                                ttgrad, vzero, workspace, workspace_bytes, spin_limit, stream);
   if (rc != kOk) return rc;
   return fteik_workspace_status(workspace, stream);
+}
+
+// ------------------------------------------------------------ batch of models --
+
+namespace {
+
+struct Batch3Layout {
+  size_t status, models, jobs, items, params, src, grads, progress, noskip, coef, rec, total;
+  long long njobs, items_max, progress_len, coef_nodes, rec_nodes;
+};
+
+Batch3Layout batch_layout(int nmodel, const int* dims, const int* nsrc, int grad) {
+  Batch3Layout L{};
+  L.njobs = 0;
+  L.items_max = 0;
+  L.progress_len = 0;
+  L.coef_nodes = 0;
+  L.rec_nodes = 0;
+  for (int m = 0; m < nmodel; ++m) {
+    const long long NZ = dims[3 * m] + 1, NX = dims[3 * m + 1] + 1, NY = dims[3 * m + 2] + 1;
+    const long long np = max_pencils((int)NX, (int)NY);
+    L.njobs += nsrc[m];
+    L.items_max += np * nsrc[m];
+    L.progress_len += np * nsrc[m];
+    L.coef_nodes += NZ * NX * NY;
+    L.rec_nodes += NZ * NX * NY * nsrc[m];
+  }
+  size_t off = 0;
+  L.status = off;
+  off = align_up(off + 16);
+  L.models = off;
+  off = align_up(off + sizeof(Model3) * (size_t)nmodel);
+  L.jobs = off;
+  off = align_up(off + sizeof(Job3) * (size_t)L.njobs);
+  L.items = off;
+  off = align_up(off + sizeof(int2) * (size_t)L.items_max);
+  L.params = off;
+  off = align_up(off + sizeof(Source3) * (size_t)L.njobs);
+  L.src = off;
+  off = align_up(off + sizeof(double) * 3 * (size_t)L.njobs);
+  L.grads = off;
+  off = align_up(off + sizeof(double*) * (size_t)L.njobs);
+  L.progress = off;
+  off = align_up(off + sizeof(unsigned) * (size_t)L.progress_len);
+  L.noskip = off;
+  off = align_up(off + sizeof(int) * (size_t)nmodel);
+  L.coef = off;
+  off = align_up(off + sizeof(double) * kNumCoef * (size_t)L.coef_nodes);
+  L.rec = off;
+  if (grad) off = align_up(off + (size_t)L.rec_nodes);
+  L.total = off;
+  return L;
+}
+
+std::vector<long long> batch_key(int nmodel, const int* dims, const int* nsrc, int grad) {
+  std::vector<long long> k{1, nmodel, grad == 1};
+  for (int m = 0; m < nmodel; ++m) {
+    k.push_back(dims[3 * m]);
+    k.push_back(dims[3 * m + 1]);
+    k.push_back(dims[3 * m + 2]);
+    k.push_back(nsrc[m]);
+  }
+  return k;
+}
+
+}  // namespace
+
+extern "C" size_t fteik3d_batch_workspace_bytes(int nmodel, const int* dims, const int* nsrc,
+                                                int grad) {
+  if (nmodel < 1 || !dims || !nsrc) return 0;
+  for (int m = 0; m < nmodel; ++m)
+    if (dims[3 * m] < 1 || dims[3 * m + 1] < 1 || dims[3 * m + 2] < 1 || nsrc[m] < 1) return 0;
+  return batch_layout(nmodel, dims, nsrc, grad ? 1 : 0).total;
+}
+
+static int solve_batch_impl(int nmodel, const double* const* slow, const int* dims,
+                            const double* spacing, const double* sources, const int* nsrc,
+                            int nsweep, int grad, double* const* tt, double* const* ttgrad,
+                            double* vzero, void* workspace, size_t workspace_bytes,
+                            long long spin_limit, void* stream, const Tune3* force) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nmodel < 1 || !slow || !dims || !spacing || !sources || !nsrc || nsweep < 0 || !tt ||
+      !vzero || !workspace || grad < 0 || grad > 1 || (grad == 1 && !ttgrad))
+    return kInvalidArgument;
+  long long total_src = 0;
+  for (int m = 0; m < nmodel; ++m) {
+    const double dz = spacing[3 * m], dx = spacing[3 * m + 1], dy = spacing[3 * m + 2];
+    if (dims[3 * m] < 2 || dims[3 * m + 1] < 2 || dims[3 * m + 2] < 2 || nsrc[m] < 1 ||
+        !slow[m] || !tt[m] || (grad == 1 && !ttgrad[m]))
+      return kInvalidArgument;
+    if (!(dz > 1e-100 && dz < 1e100 && dx > 1e-100 && dx < 1e100 && dy > 1e-100 && dy < 1e100))
+      return kInvalidArgument;
+    for (int s = 0; s < nsrc[m]; ++s) {
+      const double* p = sources + 3 * (total_src + s);
+      const bool ok = (0.0 <= p[0] && p[0] <= dz * dims[3 * m]) &&
+                      (0.0 <= p[1] && p[1] <= dx * dims[3 * m + 1]) &&
+                      (0.0 <= p[2] && p[2] <= dy * dims[3 * m + 2]);
+      if (!ok) return kSourceOutOfBound;
+    }
+    total_src += nsrc[m];
+  }
+  const Batch3Layout L = batch_layout(nmodel, dims, nsrc, grad);
+  if (workspace_bytes < L.total) return kWorkspaceTooSmall;
+  const Tune3 tune = force ? *force : resolve_tune(batch_key(nmodel, dims, nsrc, grad),
+                                                   (int)(total_src / nmodel));
+  const int pw = tune.pencil, pk = 32 / pw;
+  char* ws = (char*)workspace;
+
+  // Host tables: models, jobs, and one sweep's work items ordered by pencil
+  // diagonal, then job, so that every model's wavefront advances together
+  // and every dependency of an item has a smaller ticket.
+  std::vector<Model3> models(nmodel);
+  std::vector<Job3> jobs((size_t)L.njobs);
+  std::vector<double*> grads((size_t)L.njobs, nullptr);
+  double* coef = (double*)(ws + L.coef);
+  uint8_t* rec = grad ? (uint8_t*)(ws + L.rec) : nullptr;
+  unsigned* progress = (unsigned*)(ws + L.progress);
+  int* noskip = (int*)(ws + L.noskip);
+  long long epochs_steps_max = 0;
+  int max_diag = 0;
+  {
+    long long job = 0, poff = 0;
+    for (int m = 0; m < nmodel; ++m) {
+      Model3& M = models[m];
+      std::memset((void*)&M, 0, sizeof(M));
+      M.nz = dims[3 * m];
+      M.nx = dims[3 * m + 1];
+      M.ny = dims[3 * m + 2];
+      M.NZ = M.nz + 1;
+      M.NX = M.nx + 1;
+      M.NY = M.ny + 1;
+      M.nodes = (long long)M.NZ * M.NX * M.NY;
+      M.o = make_ops3(spacing[3 * m], spacing[3 * m + 1], spacing[3 * m + 2]);
+      M.slow = slow[m];
+      M.no_skip = noskip + m;
+      M.keep_test = keep_test_enabled(spacing[3 * m], spacing[3 * m + 1], spacing[3 * m + 2]);
+      M.PJ = (M.NX + pw - 1) / pw;
+      M.PK = (M.NY + pk - 1) / pk;
+      M.T = M.NZ + pw + pk - 2;
+      M.stride = (unsigned)M.T + 1;
+      double** fields[kNumCoef] = {&M.C.z1,  &M.C.x1,  &M.C.y1,  &M.C.zxa, &M.C.zxb,
+                                   &M.C.zxq, &M.C.zya, &M.C.zyb, &M.C.zyq, &M.C.xya,
+                                   &M.C.xyb, &M.C.xyq, &M.C.t3};
+      for (int f = 0; f < kNumCoef; ++f) *fields[f] = coef + (size_t)f * M.nodes;
+      coef += (size_t)kNumCoef * M.nodes;
+      epochs_steps_max = std::max(epochs_steps_max, (long long)M.stride);
+      max_diag = std::max(max_diag, M.PJ + M.PK - 1);
+      if (M.PJ >= (1 << 15) || M.PK >= (1 << 16)) return kInvalidArgument;
+      for (int s = 0; s < nsrc[m]; ++s, ++job) {
+        Job3& J = jobs[(size_t)job];
+        J.model = m;
+        J.pad = 0;
+        J.tt = tt[m] + (size_t)s * M.nodes;
+        J.rec = rec;
+        if (rec) rec += M.nodes;
+        J.prog = progress + poff;
+        poff += (long long)M.PJ * M.PK;
+        if (grad == 1) grads[(size_t)job] = ttgrad[m] + (size_t)3 * s * M.nodes;
+      }
+    }
+  }
+  std::vector<int2> items;
+  items.reserve((size_t)L.items_max);
+  for (int d = 0; d < max_diag; ++d)
+    for (long long q = 0; q < L.njobs; ++q) {
+      const Model3& M = models[jobs[(size_t)q].model];
+      for (int JL = std::max(0, d - M.PK + 1); JL <= std::min(d, M.PJ - 1); ++JL)
+        items.push_back(make_int2((int)q, (JL << 16) | (d - JL)));
+    }
+  const unsigned long long nepochs = 8ull * nsweep;
+  if (nepochs * epochs_steps_max >= (1ull << 31) || nepochs * items.size() >= (1ull << 31))
+    return kInvalidArgument;
+
+  Model3* d_models = (Model3*)(ws + L.models);
+  Job3* d_jobs = (Job3*)(ws + L.jobs);
+  int2* d_items = (int2*)(ws + L.items);
+  Source3* params = (Source3*)(ws + L.params);
+  double* src_dev = (double*)(ws + L.src);
+  double** d_grads = (double**)(ws + L.grads);
+  FTEIK_CHECK(cudaMemsetAsync(ws + L.status, 0, 16, st));
+  FTEIK_CHECK(cudaMemsetAsync(noskip, 0, sizeof(int) * (size_t)nmodel, st));
+  FTEIK_CHECK(cudaMemsetAsync(progress, 0, sizeof(unsigned) * (size_t)L.progress_len, st));
+  FTEIK_CHECK(cudaMemcpyAsync(d_models, models.data(), sizeof(Model3) * models.size(),
+                              cudaMemcpyHostToDevice, st));
+  FTEIK_CHECK(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(Job3) * jobs.size(),
+                              cudaMemcpyHostToDevice, st));
+  FTEIK_CHECK(cudaMemcpyAsync(d_items, items.data(), sizeof(int2) * items.size(),
+                              cudaMemcpyHostToDevice, st));
+  FTEIK_CHECK(cudaMemcpyAsync(src_dev, sources, sizeof(double) * 3 * (size_t)L.njobs,
+                              cudaMemcpyHostToDevice, st));
+  if (grad == 1)
+    FTEIK_CHECK(cudaMemcpyAsync(d_grads, grads.data(), sizeof(double*) * grads.size(),
+                                cudaMemcpyHostToDevice, st));
+  // The pageable copies above return once the host tables are staged; wait
+  // for them before the vectors go out of scope.
+  FTEIK_CHECK(cudaStreamSynchronize(st));
+  const bool use_coef = tune.coef != 0;
+  long long max_nodes = 0;
+  for (const Model3& M : models) max_nodes = std::max(max_nodes, M.nodes);
+  const int bx = std::max(1, std::min(grid_for(max_nodes, 256), 4096));
+  coef3d_batch_kernel<<<dim3(bx, nmodel), 256, 0, st>>>(d_models, use_coef);
+  fill3d_batch_kernel<<<dim3(bx, (unsigned)L.njobs), 256, 0, st>>>(d_models, d_jobs);
+  init3d_batch_kernel<<<(unsigned)((L.njobs + 63) / 64), 64, 0, st>>>(
+      d_models, d_jobs, (int)L.njobs, src_dev, params, vzero);
+  FTEIK_CHECK(cudaGetLastError());
+  if (nsweep > 0) {
+    Sweep3Args A;
+    sweep_args_defaults(A);
+    A.models = d_models;
+    A.jobs = d_jobs;
+    A.items = d_items;
+    A.items_per_epoch = (unsigned)items.size();
+    A.ticket = (unsigned*)(ws + L.status + 4);
+    A.status = (int*)(ws + L.status);
+    A.nepochs = (int)nepochs;
+    A.chunk = tune.chunk;
+    A.spin_limit = spin_limit > 0 ? spin_limit : (1LL << 25);
+    const int rc = launch_sweep(sweep_kernel(grad, use_coef, pw, true), A,
+                                (long long)nepochs * (long long)items.size(), st);
+    if (rc != kOk) return rc;
+  }
+  if (grad == 1) {
+    grad3d_batch_kernel<<<dim3(bx, (unsigned)L.njobs), 256, 0, st>>>(d_models, d_jobs, params,
+                                                                     d_grads);
+    FTEIK_CHECK(cudaGetLastError());
+  }
+  return fteik_workspace_status(workspace, stream);
+}
+
+extern "C" int fteik3d_solve_batch(int nmodel, const double* const* slow, const int* dims,
+                                   const double* spacing, const double* sources, const int* nsrc,
+                                   int nsweep, int grad, double* const* tt,
+                                   double* const* ttgrad, double* vzero, void* workspace,
+                                   size_t workspace_bytes, long long spin_limit, void* stream) {
+  return solve_batch_impl(nmodel, slow, dims, spacing, sources, nsrc, nsweep, grad, tt, ttgrad,
+                          vzero, workspace, workspace_bytes, spin_limit, stream, nullptr);
+}
+
+// ------------------------------------------------------------------ autotuner --
+
+namespace {
+
+// Coordinate search over the launch shape: chunk, then pencil width, then
+// coefficient source, each timed (sweep kernel only, CUDA events on the
+// stream) with one sweep per direction, the best of `reps` runs.
+template <class Run>
+int tune_search(Run run, int coef_sources, int reps, Tune3* best, float* best_ms) {
+  Tune3 cur{kDefaultPencil, kDefaultChunk, coef_sources >= kCoefMinSources ? 1 : 0};
+  float cur_ms = 0.f;
+  auto time_of = [&](const Tune3& t, float* ms) -> int {
+    float b = 3.4e38f;
+    for (int r = 0; r < reps; ++r) {
+      float x = 0.f;
+      const int rc = run(t, &x);
+      if (rc != kOk) return rc;
+      b = std::min(b, x);
+    }
+    *ms = b;
+    return kOk;
+  };
+  int rc = run(cur, &cur_ms);  // warm-up (first-touch, module load)
+  if (rc != kOk) return rc;
+  rc = time_of(cur, &cur_ms);
+  if (rc != kOk) return rc;
+  const int chunks[] = {1, 2, 4, 8, 16, 32};
+  const int pencils[] = {2, 4, 8};
+  for (int pass = 0; pass < 3; ++pass) {
+    Tune3 base = cur;
+    const int n = pass == 0 ? 6 : pass == 1 ? 3 : 2;
+    for (int q = 0; q < n; ++q) {
+      Tune3 t = base;
+      if (pass == 0) t.chunk = chunks[q];
+      if (pass == 1) t.pencil = pencils[q];
+      if (pass == 2) t.coef = q;
+      if (t.chunk == cur.chunk && t.pencil == cur.pencil && t.coef == cur.coef) continue;
+      float ms = 0.f;
+      rc = time_of(t, &ms);
+      if (rc != kOk) return rc;
+      if (ms < cur_ms) {
+        cur = t;
+        cur_ms = ms;
+      }
+    }
+  }
+  *best = cur;
+  *best_ms = cur_ms;
+  return kOk;
+}
+
+// Times one call of `solve` (a launch that records the timing events).
+template <class Solve>
+int timed(Solve solve, float* ms) {
+  int rc = fteik_kernel_timing(1);
+  if (rc != kOk) return rc;
+  rc = solve();
+  if (rc != kOk) return rc;
+  return fteik_last_sweep_ms(ms);
+}
+
+}  // namespace
+
+extern "C" int fteik3d_autotune(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                                double dy, const double* sources, int nsrc, int grad, double* tt,
+                                double* ttgrad, double* vzero, void* workspace,
+                                size_t workspace_bytes, long long spin_limit, int* shape,
+                                float* best_ms, void* stream) {
+  if (grad < 0 || grad > 1) return kInvalidArgument;
+  auto run = [&](const Tune3& t, float* ms) {
+    return timed(
+        [&]() {
+          int rc = solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, 1, grad, tt, ttgrad,
+                                vzero, workspace, workspace_bytes, nullptr, nullptr, spin_limit,
+                                stream, &t);
+          if (rc != kOk) return rc;
+          return fteik_workspace_status(workspace, stream);
+        },
+        ms);
+  };
+  Tune3 best;
+  float ms = 0.f;
+  const bool timing_was_on = kernel_timing_on();
+  const int rc = tune_search(run, nsrc, 2, &best, &ms);
+  fteik_kernel_timing(timing_was_on ? 1 : 0);
+  if (rc != kOk) return rc;
+  tuned_store(single_key(nz, nx, ny, nsrc, grad), best);
+  if (shape) {
+    shape[0] = best.pencil;
+    shape[1] = best.chunk;
+    shape[2] = best.coef;
+  }
+  if (best_ms) *best_ms = ms;
+  return kOk;
+}
+
+extern "C" int fteik3d_batch_autotune(int nmodel, const double* const* slow, const int* dims,
+                                      const double* spacing, const double* sources,
+                                      const int* nsrc, int grad, double* const* tt,
+                                      double* const* ttgrad, double* vzero, void* workspace,
+                                      size_t workspace_bytes, long long spin_limit, int* shape,
+                                      float* best_ms, void* stream) {
+  if (nmodel < 1 || !nsrc || grad < 0 || grad > 1) return kInvalidArgument;
+  long long total = 0;
+  for (int m = 0; m < nmodel; ++m) total += nsrc[m];
+  auto run = [&](const Tune3& t, float* ms) {
+    return timed(
+        [&]() {
+          return solve_batch_impl(nmodel, slow, dims, spacing, sources, nsrc, 1, grad, tt,
+                                  ttgrad, vzero, workspace, workspace_bytes, spin_limit, stream,
+                                  &t);
+        },
+        ms);
+  };
+  Tune3 best;
+  float ms = 0.f;
+  const bool timing_was_on = kernel_timing_on();
+  const int rc = tune_search(run, (int)(total / nmodel), 1, &best, &ms);
+  fteik_kernel_timing(timing_was_on ? 1 : 0);
+  if (rc != kOk) return rc;
+  tuned_store(batch_key(nmodel, dims, nsrc, grad), best);
+  if (shape) {
+    shape[0] = best.pencil;
+    shape[1] = best.chunk;
+    shape[2] = best.coef;
+  }
+  if (best_ms) *best_ms = ms;
+  return kOk;
+}
+
+extern "C" int fteik_clear_tuning(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned.clear();
+  return kOk;
 }

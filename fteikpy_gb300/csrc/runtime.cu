@@ -61,12 +61,14 @@ int grid_for(long long n, int threads) {
   return (int)blocks;
 }
 
-static long long g_options[kOptCount] = {-1};
+static long long g_options[kOptCount] = {-1, -1, -1, -1};
 
 long long option_value(int opt) { return (opt >= 0 && opt < kOptCount) ? g_options[opt] : -1; }
 
 static thread_local bool g_timing = false;
 static thread_local cudaEvent_t g_ev[2] = {nullptr, nullptr};
+
+bool kernel_timing_on() { return g_timing; }
 
 void timing_events(cudaEvent_t* start, cudaEvent_t* stop) {
   *start = g_timing ? g_ev[0] : nullptr;
@@ -95,7 +97,32 @@ extern "C" int fteik_set_option(const char* name, long long value) {
     g_options[kOptSweepCoef] = value < 0 ? -1 : (value ? 1 : 0);
     return kOk;
   }
+  if (std::strcmp(name, "sweep_pencil") == 0) {
+    if (value >= 0 && value != 2 && value != 4 && value != 8) return kInvalidArgument;
+    g_options[kOptSweepPencil] = value < 0 ? -1 : value;
+    return kOk;
+  }
+  if (std::strcmp(name, "sweep_chunk") == 0) {
+    if (value >= 0 && (value < 1 || value > 64 || (value & (value - 1)) != 0))
+      return kInvalidArgument;
+    g_options[kOptSweepChunk] = value < 0 ? -1 : value;
+    return kOk;
+  }
+  if (std::strcmp(name, "sweep_keep_test") == 0) {
+    g_options[kOptKeepTest] = value < 0 ? -1 : (value ? 1 : 0);
+    return kOk;
+  }
   return kInvalidArgument;
+}
+
+extern "C" int fteik_get_option(const char* name, long long* value) {
+  if (!name || !value) return kInvalidArgument;
+  if (std::strcmp(name, "sweep_coef") == 0) *value = g_options[kOptSweepCoef];
+  else if (std::strcmp(name, "sweep_pencil") == 0) *value = g_options[kOptSweepPencil];
+  else if (std::strcmp(name, "sweep_chunk") == 0) *value = g_options[kOptSweepChunk];
+  else if (std::strcmp(name, "sweep_keep_test") == 0) *value = g_options[kOptKeepTest];
+  else return kInvalidArgument;
+  return kOk;
 }
 
 extern "C" int fteik_kernel_timing(int on) {

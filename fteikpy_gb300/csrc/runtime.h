@@ -26,11 +26,15 @@ int grid_for(long long n, int threads);
 // When kernel timing is on (fteik_kernel_timing), the pair of events that the
 // 3D solve records around its sweep kernel on the launching stream; else null.
 void timing_events(cudaEvent_t* start, cudaEvent_t* stop);
+bool kernel_timing_on();
 
 // Tuning options (fteik_set_option); -1 = automatic.
 enum Option : int {
-  kOptSweepCoef = 0,  // 3D sweep coefficients: 1 precomputed arrays, 0 slowness cells
-  kOptCount = 1,
+  kOptSweepCoef = 0,    // 3D sweep coefficients: 1 precomputed arrays, 0 slowness cells
+  kOptSweepPencil = 1,  // 3D pencil width along x: 2, 4 or 8 (the pencil is w x 32/w)
+  kOptSweepChunk = 2,   // 3D steps between progress publications: 1, 2, 4, ... 64
+  kOptKeepTest = 3,     // 3D unchanged-node test before the 2D/3D operators: 0 off
+  kOptCount = 4,
 };
 long long option_value(int opt);
 

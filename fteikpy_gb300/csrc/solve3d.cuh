@@ -8,8 +8,21 @@
 
 namespace fteik {
 
-constexpr int kPJ = 4;  // pencil width along x (j)
-constexpr int kPK = 8;  // pencil width along y (k)
+// A pencil is PW x 32/PW node columns (x by y), one per warp lane.
+constexpr int kDefaultPencil = 4;
+constexpr int kDefaultChunk = 4;
+
+inline int pencils_of(int NX, int NY, int pw) {
+  const int pk = 32 / pw;
+  return ((NX + pw - 1) / pw) * ((NY + pk - 1) / pk);
+}
+// Pencil count of the largest of the supported shapes (2, 4 or 8 wide).
+inline int max_pencils(int NX, int NY) {
+  int m = pencils_of(NX, NY, 2);
+  if (pencils_of(NX, NY, 4) > m) m = pencils_of(NX, NY, 4);
+  if (pencils_of(NX, NY, 8) > m) m = pencils_of(NX, NY, 8);
+  return m;
+}
 
 struct Ops3 {
   double dz, dx, dy, dz2i, dx2i, dy2i, dz2dx2, dz2dy2, dx2dy2, dsum;
@@ -92,7 +105,7 @@ struct Layout3 {
 inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 inline Layout3 layout3(int nz, int nx, int ny, int nsrc, int grad) {
-  const int PJ = (nx + 1 + kPJ - 1) / kPJ, PK = (ny + 1 + kPK - 1) / kPK;
+  const size_t npen = (size_t)max_pencils(nx + 1, ny + 1);
   const size_t nodes = (size_t)(nz + 1) * (nx + 1) * (ny + 1);
   Layout3 L;
   size_t off = 0;
@@ -103,9 +116,9 @@ inline Layout3 layout3(int nz, int nx, int ny, int nsrc, int grad) {
   L.src = off;
   off = align_up(off + sizeof(double) * 3 * (size_t)nsrc);
   L.order = off;
-  off = align_up(off + sizeof(int) * (size_t)PJ * PK);
+  off = align_up(off + sizeof(int) * npen);
   L.progress = off;
-  off = align_up(off + sizeof(unsigned) * (size_t)PJ * PK * nsrc);
+  off = align_up(off + sizeof(unsigned) * npen * nsrc);
   L.coef = off;
   off = align_up(off + sizeof(double) * nodes * kNumCoef);
   L.rec = off;

@@ -41,11 +41,17 @@ const char* fteik_last_error(void);
  * kernel's duration. fteik_fp64_peak times a DFMA loop (nblocks x 256 threads,
  * 4 chains each; `scratch` holds nblocks*256 doubles) and returns FLOP/s. */
 int fteik_kernel_timing(int on);
-/* Tuning knobs (no counterpart in the reference). "sweep_coef": -1 chooses
- * automatically, 0 makes the 3D sweep derive its slowness factors from the
+/* Tuning knobs (no counterpart in the reference); -1 chooses automatically.
+ * "sweep_coef": 0 makes the 3D sweep derive its slowness factors from the
  * 8 cells around each node, 1 makes it read precomputed coefficient arrays
- * (faster for batches of sources, which reuse them). Results are identical. */
+ * (faster for batches of sources, which reuse them). "sweep_pencil": pencil
+ * width along x, 2, 4 or 8. "sweep_chunk": steps between progress
+ * publications, a power of 2 up to 64. "sweep_keep_test": 0 turns off the
+ * test that skips the 2D/3D operators of nodes that provably keep their value
+ * (grids with equal spacings only). Results are identical for every setting.
+ * fteik_get_option reads a knob back. */
 int fteik_set_option(const char* name, long long value);
+int fteik_get_option(const char* name, long long* value);
 int fteik_last_sweep_ms(float* ms);
 int fteik_fp64_peak(double* scratch, int nblocks, int iters, double* flops_per_s, void* stream);
 
@@ -90,6 +96,55 @@ int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, double dz, d
 /* Synchronise `stream` and return the device-side status of the last solve
  * enqueued with this workspace. */
 int fteik_workspace_status(const void* workspace, void* stream);
+
+/* ------------------------------------------------------ batch of 3D models --
+ * No single counterpart in the reference: there, each model is an Eikonal3D
+ * and each solve a fteik3d_vectorized call (fteikpy/_fteik/_fteik3d.py:493-513)
+ * over that model's sources. Here models of different sizes and spacings,
+ * each with its own sources, are solved by ONE persistent sweep launch.
+ *  slow      HOST [nmodel] array of device pointers, model m [nz][nx][ny]
+ *  dims      HOST [nmodel][3] cell counts (nz, nx, ny), each >= 2
+ *  spacing   HOST [nmodel][3] (dz, dx, dy)
+ *  sources   HOST [sum nsrc][3], model by model, relative to each origin
+ *  nsrc      HOST [nmodel] sources per model (>= 1)
+ *  tt        HOST [nmodel] array of device pointers, model m
+ *            [nsrc[m]][nz+1][nx+1][ny+1]
+ *  ttgrad    HOST [nmodel] array of device pointers ([..][3]) or NULL when
+ *            grad == 0 (grad is 0 or 1 here)
+ *  vzero     device [sum nsrc]
+ *  workspace device scratch of fteik3d_batch_workspace_bytes(...) bytes
+ * Results equal those of one fteik3d_solve per model. Blocking. */
+size_t fteik3d_batch_workspace_bytes(int nmodel, const int* dims, const int* nsrc, int grad);
+int fteik3d_solve_batch(int nmodel, const double* const* slow, const int* dims,
+                        const double* spacing, const double* sources, const int* nsrc,
+                        int nsweep, int grad, double* const* tt, double* const* ttgrad,
+                        double* vzero, void* workspace, size_t workspace_bytes,
+                        long long spin_limit, void* stream);
+
+/* ----------------------------------------------------------------- autotuner --
+ * Launch shape of the 3D sweep kernel: pencil width along x (2, 4 or 8; a
+ * pencil is w x 32/w node columns, one per lane of a warp), steps between
+ * progress publications (a power of 2, the hyperplane chunk), and the
+ * coefficient source (1 precomputed arrays, 0 slowness cells). The autotuner
+ * times candidate shapes on the caller's problem (one sweep per direction,
+ * sweep kernel only), keeps the fastest for that problem signature (cell
+ * counts, source counts, gradients) for the rest of the process, and returns
+ * it in shape[3] = {pencil, chunk, coef} and its time in best_ms. Solves of
+ * the same signature then use it unless fteik_set_option overrides a part
+ * ("sweep_pencil", "sweep_chunk", "sweep_coef"; -1 = automatic). The
+ * arguments are those of fteik3d_solve / fteik3d_solve_batch (the outputs are
+ * overwritten). No counterpart in the reference. */
+int fteik3d_autotune(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,
+                     const double* sources, int nsrc, int grad, double* tt, double* ttgrad,
+                     double* vzero, void* workspace, size_t workspace_bytes, long long spin_limit,
+                     int* shape, float* best_ms, void* stream);
+int fteik3d_batch_autotune(int nmodel, const double* const* slow, const int* dims,
+                           const double* spacing, const double* sources, const int* nsrc,
+                           int grad, double* const* tt, double* const* ttgrad, double* vzero,
+                           void* workspace, size_t workspace_bytes, long long spin_limit,
+                           int* shape, float* best_ms, void* stream);
+/* Forget every measured shape. */
+int fteik_clear_tuning(void);
 
 /* 3D solve that allocates nothing. No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc or hand over a device workspace (a

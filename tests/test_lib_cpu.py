@@ -141,3 +141,59 @@ def test_resample_and_smooth_match_reference_semantics():
     eik2 = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
     eik2.smooth(1.0)
     assert eik2.grid.sum() == eik2.grid.size
+
+
+def _batch_args(dims, nsrc, sources, spacing=None):
+    n = len(dims)
+    P = ctypes.c_void_p * n
+    dims = np.ascontiguousarray(dims, dtype=np.int32)
+    nsrc = np.ascontiguousarray(nsrc, dtype=np.int32)
+    spacing = np.ascontiguousarray(spacing if spacing is not None else np.ones((n, 3)))
+    sources = np.ascontiguousarray(sources, dtype=np.float64)
+    return n, P(*[FAKE] * n), dims, spacing, sources, nsrc, P(*[FAKE] * n)
+
+
+def test_batch_workspace_and_host_checks(lib):
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    dims = [[4, 5, 6], [9, 3, 7]]
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    one = np.ascontiguousarray([1, 1], dtype=np.int32)
+    two = np.ascontiguousarray([20, 30], dtype=np.int32)
+    b1 = lib.fteik3d_batch_workspace_bytes(2, p(d), p(one), 0)
+    assert b1 > 0 and b1 % 256 == 0
+    assert lib.fteik3d_batch_workspace_bytes(2, p(d), p(two), 0) > b1
+    assert lib.fteik3d_batch_workspace_bytes(2, p(d), p(two), 1) > lib.fteik3d_batch_workspace_bytes(
+        2, p(d), p(two), 0)
+    bad = np.ascontiguousarray([[4, 5, 6], [0, 3, 7]], dtype=np.int32)
+    assert lib.fteik3d_batch_workspace_bytes(2, p(bad), p(one), 0) == 0
+    assert lib.fteik3d_batch_workspace_bytes(0, p(d), p(one), 0) == 0
+
+    def solve(sources, nsrc=(1, 1), grad=0, ws=None, dims=dims):
+        n, slow, dd, sp, src, ns, tt = _batch_args(dims, nsrc, sources)
+        wsb = ws if ws is not None else lib.fteik3d_batch_workspace_bytes(n, p(dd), p(ns), grad)
+        return lib.fteik3d_solve_batch(n, slow, p(dd), p(sp), p(src), p(ns), 2, grad, tt,
+                                       tt if grad else None, FAKE, FAKE, wsb, 0, None)
+
+    # model 1 is 9 x 3 x 7 cells of 1 m: z = 9.5 is outside
+    assert solve([[0.0, 0.0, 0.0], [9.5, 0.0, 0.0]]) == _lib.SOURCE_OUT_OF_BOUND
+    assert solve([[4.5, 0.0, 0.0], [0.0, 0.0, 0.0]]) == _lib.SOURCE_OUT_OF_BOUND
+    assert solve([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]], ws=256) == _lib.WORKSPACE_TOO_SMALL
+    assert solve([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]], grad=2) == _lib.INVALID_ARGUMENT
+    assert solve([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0]],
+                 dims=[[4, 5, 6], [1, 3, 7]]) == _lib.INVALID_ARGUMENT
+
+
+def test_tuning_options_host_side(lib):
+    v = ctypes.c_longlong()
+    for name, good, bad in ((b"sweep_pencil", (2, 4, 8), (1, 3, 16)),
+                            (b"sweep_chunk", (1, 2, 64), (3, 0, 128)),
+                            (b"sweep_coef", (0, 1), ()),
+                            (b"sweep_keep_test", (0, 1), ())):
+        for g in good:
+            assert lib.fteik_set_option(name, g) == 0
+            assert lib.fteik_get_option(name, ctypes.byref(v)) == 0 and v.value == g
+        for b in bad:
+            assert lib.fteik_set_option(name, b) == _lib.INVALID_ARGUMENT
+        assert lib.fteik_set_option(name, -1) == 0
+    assert lib.fteik_set_option(b"no_such_option", 1) == _lib.INVALID_ARGUMENT
+    assert lib.fteik_clear_tuning() == 0

@@ -87,9 +87,10 @@ class _Traveltimes(torch.autograd.Function):
         ax = ctx.axes
         rc = lib.fteik3d_adjoint(
             _device.ptr(slow), nz, nx, ny, *ctx.gridsize, nsrc, ctx.nsweep, _device.ptr(tt),
-            _device.ptr(ws), ws.numel(), _device.ptr(tape), tape.numel(), _device.ptr(ax[0]), _device.ptr(ax[1]), _device.ptr(ax[2]),
+            _device.ptr(ws), ws.numel(), _device.ptr(tape), tape.numel(), _device.ptr(ax[0]),
+            _device.ptr(ax[1]), _device.ptr(ax[2]),
             _device.ptr(src_dev), _device.ptr(rec), rec.shape[0], _device.ptr(g),
-            _device.ptr(grad_slow), _device.ptr(aws), aws.numel(), _device.stream(),
+            _device.ptr(grad_slow), _device.ptr(aws), aws.numel(), SPIN_LIMIT, _device.stream(),
         )
         _lib.check(rc, "traveltimes backward")
         # slowness = 1 / velocity, so dL/dv = -dL/ds * s^2

@@ -53,7 +53,7 @@ SIGNATURES = {
     "fteik3d_adjoint": (
         _I,
         [_P, _I, _I, _I, _D, _D, _D, _I, _I, _P, _P, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _I, _P,
-         _P, _P, _SZ, _P],
+         _P, _P, _SZ, _LL, _P],
     ),
     "fteik2d_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
     "fteik2d_solve": (_I, [_P, _I, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _P]),

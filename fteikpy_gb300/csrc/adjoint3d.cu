@@ -16,6 +16,7 @@
 // those inputs, books the slowness term, and restores its previous value.
 // Every transfer is a pull or a per-node accumulation, so the result is the
 // same from run to run.
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -92,7 +93,7 @@ __device__ void linearize(int az, int ax, int ay, int i, int j, int k, long long
   const int km = imax(k - 1, 0), kp = imin(k, A.ny - 1);
   const int i1 = az > 0 ? i - 1 : i, j1 = ax > 0 ? j - 1 : j, k1 = ay > 0 ? k - 1 : k;
 #define C(a, b, c) (((a)*A.nx + (b)) * A.ny + (c))
-#define T(bz, bx, by) t[n - (long long)(bz) * az * NXY - (long long)(bx) * ax * A.NY - (by) * ay]
+#define T(bz, bx, by) __ldcg(t + n - (long long)(bz) * az * NXY - (long long)(bx) * ax * A.NY - (by) * ay)
   const int nnz = (az != 0) + (ax != 0) + (ay != 0);
   if (nnz == 1) {
     int cells[4];
@@ -202,64 +203,153 @@ __device__ __forceinline__ int cell_slot(int i, int j, int k, int ci, int cj, in
   return a * 4 + b * 2 + c;
 }
 
-// One hyperplane of one sweep, in reverse.  In sweep e (signs sz, sx, sy) the
-// node at local coordinates (ii, jj, kk) was updated after every node of a
-// smaller ii + jj + kk; going back, plane h runs after the planes above it.
-// A node first collects what its readers of this sweep sent it (they lie
+// One node of one sweep, in reverse.  In sweep e (signs sz, sx, sy) the node
+// at local coordinates (ii, jj, kk) was updated after every node of a smaller
+// ii + jj + kk; going back, its hyperplane runs after the planes above it.
+// The node first collects what its readers of this sweep sent it (they lie
 // downwind, on planes already done), then, if this sweep changed it,
 // linearises the operator at the values it read, sends the adjoint on to its
-// inputs, books the slowness term and restores its previous value.
-__global__ void adj_reverse_plane_kernel(const RevArgs A, int e, int h) {
+// inputs, books the slowness term and restores its previous value.  Arrays
+// other threads write are read through L2 (ld.global.cg).
+__device__ __forceinline__ void reverse_node(const RevArgs& A, int e, int src, int ii, int jj,
+                                             int kk) {
   const int dir = e & 7;
   const int sz = dir < 4 ? 1 : -1, sx = (dir & 1) ? -1 : 1, sy = (dir & 2) ? -1 : 1;
   const long long NXY = (long long)A.NX * A.NY;
-  const long long total = (long long)A.nsrc * NXY;
-  for (long long q0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; q0 < total;
-       q0 += (long long)gridDim.x * blockDim.x) {
-    const int src = (int)(q0 / NXY);
-    const long long jk = q0 - (long long)src * NXY;
-    const int jj = (int)(jk / A.NY), kk = (int)(jk - (long long)jj * A.NY);
-    const int ii = h - jj - kk;
-    if (ii < 0 || ii >= A.NZ) continue;
-    const int i = sz > 0 ? ii : A.NZ - 1 - ii;
-    const int j = sx > 0 ? jj : A.NX - 1 - jj;
-    const int k = sy > 0 ? kk : A.NY - 1 - kk;
-    const long long n = (long long)i * NXY + (long long)j * A.NY + k;
-    const long long base = (long long)src * A.nodes;
-    const long long tbase = ((long long)e * A.nsrc + src) * A.nodes;
-    double lam = A.lam[base + n];
-    for (int slot = 0; slot < kSlots; ++slot) {
-      const int bz = (slot + 1) >> 2, bx = ((slot + 1) >> 1) & 1, by = (slot + 1) & 1;
-      const int mi = i + bz * sz, mj = j + bx * sx, mk = k + by * sy;
-      if (mi < 0 || mi >= A.NZ || mj < 0 || mj >= A.NX || mk < 0 || mk >= A.NY) continue;
-      const long long m = (long long)mi * NXY + (long long)mj * A.NY + mk;
-      const int code = A.tcode[tbase + m];
-      if (code == 255) continue;
-      int az, ax, ay;
-      decode(code, az, ax, ay);
-      if ((bz && !az) || (bx && !ax) || (by && !ay)) continue;
-      lam += A.contrib[(base + m) * kSlots + slot];
-    }
-    const int code = A.tcode[tbase + n];
-    if (code == 255) {
-      A.lam[base + n] = lam;
-      continue;
-    }
-    int az, ax, ay;
-    decode(code, az, ax, ay);
-    double w[kSlots], ps;
-    int cell[4], ncell;
-    linearize(az, ax, ay, i, j, k, n, A.tt + base, A.slow, A.nz, A.nx, A.ny, A.NX, A.NY, A.o, w,
-              ps, cell, ncell);
-    double* c = A.contrib + (base + n) * kSlots;
+  const int i = sz > 0 ? ii : A.NZ - 1 - ii;
+  const int j = sx > 0 ? jj : A.NX - 1 - jj;
+  const int k = sy > 0 ? kk : A.NY - 1 - kk;
+  const long long n = (long long)i * NXY + (long long)j * A.NY + k;
+  const long long base = (long long)src * A.nodes;
+  const long long tbase = ((long long)e * A.nsrc + src) * A.nodes;
+  // All reads are issued before any is used, so their latencies overlap.
+  const int code = __ldg(A.tcode + tbase + n);
+  const double lam0 = __ldcg(A.lam + base + n);
+  long long m[kSlots];
+  int dcode[kSlots];
 #pragma unroll
-    for (int slot = 0; slot < kSlots; ++slot) c[slot] = lam * w[slot];
-    for (int q = 0; q < ncell; ++q) {
-      const int ci = cell[q] / (A.nx * A.ny), cj = (cell[q] / A.ny) % A.nx, ck = cell[q] % A.ny;
-      A.g8[(base + n) * 8 + cell_slot(i, j, k, ci, cj, ck)] += lam * ps;
+  for (int slot = 0; slot < kSlots; ++slot) {
+    const int bz = (slot + 1) >> 2, bx = ((slot + 1) >> 1) & 1, by = (slot + 1) & 1;
+    const int mi = i + bz * sz, mj = j + bx * sx, mk = k + by * sy;
+    const bool in = mi >= 0 && mi < A.NZ && mj >= 0 && mj < A.NX && mk >= 0 && mk < A.NY;
+    m[slot] = (long long)mi * NXY + (long long)mj * A.NY + mk;
+    dcode[slot] = in ? (int)__ldg(A.tcode + tbase + m[slot]) : 255;
+  }
+  double part[kSlots];
+#pragma unroll
+  for (int slot = 0; slot < kSlots; ++slot) {
+    const int bz = (slot + 1) >> 2, bx = ((slot + 1) >> 1) & 1, by = (slot + 1) & 1;
+    part[slot] = 0.0;
+    if (dcode[slot] == 255) continue;
+    int az, ax, ay;
+    decode(dcode[slot], az, ax, ay);
+    if ((bz && !az) || (bx && !ax) || (by && !ay)) continue;
+    part[slot] = __ldcg(A.contrib + (base + m[slot]) * kSlots + slot);
+  }
+  double lam = lam0;
+  bool pulled = false;
+#pragma unroll
+  for (int slot = 0; slot < kSlots; ++slot) {
+    if (dcode[slot] == 255) continue;
+    lam += part[slot];
+    pulled = true;
+  }
+  if (code == 255) {
+    if (pulled) A.lam[base + n] = lam;
+    return;
+  }
+  int az, ax, ay;
+  decode(code, az, ax, ay);
+  double w[kSlots], ps;
+  int cell[4], ncell;
+  linearize(az, ax, ay, i, j, k, n, A.tt + base, A.slow, A.nz, A.nx, A.ny, A.NX, A.NY, A.o, w, ps,
+            cell, ncell);
+  double* c = A.contrib + (base + n) * kSlots;
+#pragma unroll
+  for (int slot = 0; slot < kSlots; ++slot) c[slot] = lam * w[slot];
+  for (int q = 0; q < ncell; ++q) {
+    const int ci = cell[q] / (A.nx * A.ny), cj = (cell[q] / A.ny) % A.nx, ck = cell[q] % A.ny;
+    double* g = A.g8 + (base + n) * 8 + cell_slot(i, j, k, ci, cj, ck);
+    *g = __ldcg(g) + lam * ps;
+  }
+  A.lam[base + n] = 0.0;
+  A.tt[base + n] = __ldg(A.told + tbase + n);
+}
+
+// Barrier of the `nblocks` blocks of one group of a cooperative launch
+// (every block is resident). The last block to arrive resets the count and
+// publishes a new generation; the others poll the generation at most
+// spin_limit times, then flag FTEIK_DEVICE_WAIT_TIMEOUT and return false, as
+// they do once any block has flagged a failure.
+struct GridBarrier {
+  unsigned count, gen;
+};
+
+__device__ bool group_barrier(GridBarrier* b, unsigned nblocks, int* status,
+                              long long spin_limit) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = ld_acquire(&b->gen);
+    __threadfence();
+    if (atomicAdd(&b->count, 1u) + 1u == nblocks) {
+      b->count = 0;
+      __threadfence();
+      st_release(&b->gen, g + 1u);
+    } else {
+      for (long long it = 0; ld_acquire(&b->gen) == g; ++it) {
+        if (it >= spin_limit) {
+          atomicCAS(status, 0, (int)kDeviceWaitTimeout);
+          ok = 0;
+          break;
+        }
+        if ((it & 15) == 15 && *((volatile int*)status) != 0) {
+          ok = 0;
+          break;
+        }
+        if (it >= 64) __nanosleep(64);
+      }
     }
-    A.lam[base + n] = 0.0;
-    A.tt[base + n] = A.told[tbase + n];
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// Every sweep in reverse, hyperplane by hyperplane, in one cooperative
+// launch. Sources are independent, so the blocks form `ngroups` groups that
+// each take every ngroups-th source and meet only at their own barrier: per
+// plane, the group's threads share out the plane's nodes (per column jj, the
+// band of kk whose ii = h - jj - kk lies in the grid), then wait for each
+// other before the plane below.
+__global__ void __launch_bounds__(256)
+    adj_reverse_kernel(const RevArgs A, int nepochs, int ngroups, GridBarrier* bars,
+                       int* status, long long spin_limit) {
+  const int hmax = A.NZ + A.NX + A.NY - 3;
+  const int g = (int)((long long)blockIdx.x * ngroups / gridDim.x);
+  const int b0 = (int)(((long long)g * gridDim.x + ngroups - 1) / ngroups);
+  const int b1 = (int)(((long long)(g + 1) * gridDim.x + ngroups - 1) / ngroups);
+  const unsigned nb = (unsigned)(b1 - b0);
+  const long long tid = (long long)(blockIdx.x - b0) * blockDim.x + threadIdx.x;
+  const long long nthreads = (long long)nb * blockDim.x;
+  GridBarrier* bar = bars + g;
+  for (int src = g; src < A.nsrc; src += ngroups) {
+    for (int e = nepochs - 1; e >= 0; --e) {
+      for (int h = hmax; h >= 0; --h) {
+        const int jlo = imax(0, h - (A.NZ - 1) - (A.NY - 1)), jhi = imin(A.NX - 1, h);
+        const int W = imin(imin(A.NZ, A.NY), h + 1);
+        const long long total = (long long)(jhi - jlo + 1) * W;
+        for (long long q = tid; q < total; q += nthreads) {
+          const int jj = jlo + (int)(q / W);
+          const int kk = imax(0, h - jj - (A.NZ - 1)) + (int)(q % W);
+          if (kk > imin(A.NY - 1, h - jj)) continue;
+          reverse_node(A, e, src, h - jj - kk, jj, kk);
+        }
+        if (!group_barrier(bar, nb, status, spin_limit)) return;
+      }
+    }
   }
 }
 
@@ -370,7 +460,7 @@ __global__ void adj_gather_kernel(const RevArgs A, const double* vzg, double* gr
 }
 
 struct AdjLayout {
-  size_t tt, lam, contrib, g8, vzg, total;
+  size_t tt, lam, contrib, g8, vzg, sync, total;
 };
 
 static AdjLayout adj_layout(int nz, int nx, int ny, int nsrc) {
@@ -387,6 +477,8 @@ static AdjLayout adj_layout(int nz, int nx, int ny, int nsrc) {
   off = align_up(off + 8 * 8 * N);
   L.vzg = off;
   off = align_up(off + 8 * (size_t)nsrc);
+  L.sync = off;  // int status, then one barrier per source group
+  off = align_up(off + 8 + 8 * (size_t)nsrc);
   L.total = off;
   return L;
 }
@@ -407,7 +499,7 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
                                const double* ax1, const double* ax2, const double* sources,
                                const double* receivers, int nrec, const double* grad_tt_rec,
                                double* grad_slow, void* workspace, size_t workspace_bytes,
-                               void* stream) {
+                               long long spin_limit, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || nsweep < 0 || nrec < 0 || !slow || !tt ||
       !solve_workspace || !tape || !ax0 || !ax1 || !ax2 || !sources ||
@@ -448,15 +540,29 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
   adj_seed_kernel<<<(nsrc + 63) / 64, 64, 0, st>>>(A, ax0, ax1, ax2, sources, receivers, nrec,
                                                    grad_tt_rec, vzg);
   FTEIK_CHECK(cudaGetLastError());
-  const int nepochs = 8 * nsweep;
-  const int hmax = A.NZ + A.NX + A.NY - 3;
-  const int blocks = grid_for((long long)nsrc * A.NX * A.NY, 256);
-  for (int e = nepochs - 1; e >= 0; --e)
-    for (int h = hmax; h >= 0; --h) adj_reverse_plane_kernel<<<blocks, 256, 0, st>>>(A, e, h);
+  int nepochs = 8 * nsweep;
+  if (nepochs > 0) {
+    int* status = (int*)(ws + L.sync);
+    GridBarrier* bars = (GridBarrier*)(ws + L.sync + 8);
+    FTEIK_CHECK(cudaMemsetAsync(ws + L.sync, 0, 8 + sizeof(GridBarrier) * (size_t)nsrc, st));
+    const void* kern = (const void*)adj_reverse_kernel;
+    const int blocks = resident_blocks(kern, 256);
+    // one group of blocks per source while there are blocks enough
+    int ngroups = std::min(nsrc, blocks);
+    long long limit = spin_limit > 0 ? spin_limit : (1LL << 25);
+    void* args[] = {(void*)&A,    (void*)&nepochs, (void*)&ngroups,
+                    (void*)&bars, (void*)&status,  (void*)&limit};
+    FTEIK_CHECK(cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(256), args, 0, st));
+  }
   FTEIK_CHECK(cudaGetLastError());
   adj_initial_kernel<<<(nsrc * 8 + 127) / 128, 128, 0, st>>>(A);
   adj_gather_kernel<<<grid_for((long long)nz * nx * ny, 256), 256, 0, st>>>(A, vzg, grad_slow);
   FTEIK_CHECK(cudaGetLastError());
   FTEIK_CHECK(cudaStreamSynchronize(st));
+  if (nepochs > 0) {
+    int dev_status = 0;
+    FTEIK_CHECK(cudaMemcpy(&dev_status, ws + L.sync, sizeof(int), cudaMemcpyDeviceToHost));
+    if (dev_status != 0) return dev_status;
+  }
   return kOk;
 }

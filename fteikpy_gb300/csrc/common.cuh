@@ -12,10 +12,13 @@
 //    values; -0.0 never arises in these kernels);
 //  * multiplication by 0.5 or 4.0 (exact scalings) edits the exponent field;
 //  * division by a per-launch constant c uses a double-double reciprocal of c
-//    and one Markstein correction step, which returns the correctly rounded
-//    quotient (Markstein, "IA-64 and Elementary Functions", 2000, Thm. 8.?:
-//    a faithful quotient q plus r*y with r = a - b*q exact and y = RN(1/b)
-//    rounds to RN(a/b)); tests compare it against the IEEE division.
+//    and one Markstein correction step: with y = RN(1/c), a quotient q within
+//    one ulp of a/c (from the double-double product) and the exact remainder
+//    r = a - c*q (one FMA), RN(q + r*y) is the correctly rounded a/c
+//    (P. Markstein's correction theorem, IBM J. Res. Dev. 34(1), 1990; the
+//    division chapter of Muller et al., Handbook of Floating-Point
+//    Arithmetic). The bitwise tests against the oracle, which divides with
+//    IEEE `/`, check it on every solve.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>

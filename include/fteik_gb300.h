@@ -186,7 +186,10 @@ int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny, double dz,
  *  receivers   device [nrec][3], the same receivers for every source
  *  grad_tt_rec device [nsrc][nrec] d(loss)/d(traveltime at receiver)
  *  grad_slow   device [nz][nx][ny] d(loss)/d(slowness), summed over sources
- * Deterministic (no floating-point atomics). Both calls block. */
+ *  spin_limit  polls of one grid-barrier wait before the reverse pass gives
+ *              up with FTEIK_DEVICE_WAIT_TIMEOUT (<= 0: default)
+ * The reverse pass is one cooperative launch that visits every hyperplane of
+ * every sweep. Deterministic (no floating-point atomics). Both calls block. */
 size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep);
 int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, double dz, double dx,
                        double dy, const double* sources, int nsrc, int nsweep, double* tt,
@@ -199,7 +202,7 @@ int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, double dz, doubl
                     const double* ax0, const double* ax1, const double* ax2,
                     const double* sources, const double* receivers, int nrec,
                     const double* grad_tt_rec, double* grad_slow, void* workspace,
-                    size_t workspace_bytes, void* stream);
+                    size_t workspace_bytes, long long spin_limit, void* stream);
 
 /* ---------------------------------------------------------------- 2D solve --
  * Replaces solve2d / fteik2d / fteik2d_vectorized

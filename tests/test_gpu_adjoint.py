@@ -105,3 +105,25 @@ def test_adjoint_with_zero_sweeps_and_outside_receivers():
         s = 1.0 / v0
         go = -O.adjoint3d(s, D, src, nsweep, rec, To) * s * s
         assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()
+
+
+def test_reverse_pass_wait_timeout_is_reported_and_recoverable(monkeypatch):
+    """The reverse pass's grid barrier waits at most spin_limit polls: with a
+    limit of 1 it reports a timeout instead of hanging, and the next backward
+    on the same context gives the exact gradient."""
+    from fteikpy_gb300 import _adjoint
+
+    shape, nsweep = (10, 12, 11), 2
+    src, rec = geometry(shape, 3, 12, 6)
+    v0 = velocity(shape, False)
+    t_obs = oracle_times(velocity(shape, True), src, rec, nsweep)
+    vt = torch.tensor(v0, device="cuda", requires_grad=True)
+    T = fp.traveltimes(vt, D, src, rec, nsweep)
+    loss = 0.5 * ((T - torch.as_tensor(t_obs, device="cuda")) ** 2).sum()
+    monkeypatch.setattr(_adjoint, "SPIN_LIMIT", 1)
+    with pytest.raises(RuntimeError, match="timed out"):
+        loss.backward()
+    monkeypatch.undo()
+    _, g = gpu_gradient(v0, src, rec, nsweep, t_obs)
+    go = oracle_velocity_gradient(v0, src, rec, nsweep, t_obs)
+    assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()

@@ -4,6 +4,7 @@ argument meaning and errors) with device-resident storage.
 A grid's values may live on the host (NumPy), on the device (a CUDA tensor) or
 both; ``.grid`` always returns a NumPy array as in the reference (copied from
 the device once, then cached), while the compute calls use the device copy.
+Interpolation, resampling and smoothing run on the device.
 """
 
 from abc import ABC
@@ -136,7 +137,91 @@ class BaseGrid(ABC):
         return float(res[0]) if single else res
 
 
-class BaseGrid2D(BaseGrid):
+def _axis_table(axis, points, method):
+    """Per-axis lookup of scipy's RegularGridInterpolator at ``points``
+    (scipy/interpolate/_rgi.py: lower index i = searchsorted(axis, x) - 1
+    clipped to [0, n - 2], normalised distance y = (x - a[i]) / (a[i+1] - a[i]);
+    "nearest" takes i where y <= 0.5, else i + 1)."""
+    i = np.clip(np.searchsorted(axis, points, side="left") - 1, 0, len(axis) - 2)
+    y = (points - axis[i]) / (axis[i + 1] - axis[i])
+    if method == "nearest":
+        return np.where(y <= 0.5, i, i + 1).astype(np.int32), None, None
+    return i.astype(np.int32), y, 1 - y
+
+
+def _gaussian_weights(sigma, truncate=4.0):
+    """scipy.ndimage.gaussian_filter1d's kernel for order 0: radius
+    int(truncate * sigma + 0.5), exp(-x^2 / (2 sigma^2)) normalised to sum 1."""
+    r = int(truncate * float(sigma) + 0.5)
+    x = np.arange(-r, r + 1)
+    phi = np.exp(-0.5 / (sigma * sigma) * x**2)
+    return phi / phi.sum()
+
+
+class _GridOpsMixin:
+    def _resample_device(self, new_shape, method):
+        """RegularGridInterpolator(axes, grid, method, bounds_error=False) at
+        the tensor grid of np.linspace(axis[0], axis[-1], new_shape[d]), as
+        fteikpy/_base.py:81-110,165-199 builds it, evaluated by
+        ``fteik_resample``; the grid spacing follows the reference."""
+        if method not in ("linear", "nearest"):
+            raise ValueError(f"Method '{method}' is not defined")
+        nd = self._ndim
+        new_shape = tuple(int(n) for n in new_shape)
+        if len(new_shape) != nd or min(new_shape) < 1:
+            raise ValueError(f"new_shape must hold {nd} positive sizes")
+        if min(self.shape) < 2:
+            raise ValueError("resampling needs at least 2 points per dimension")
+        tables = []
+        for d in range(nd):
+            axis = self._axis(d)
+            q = np.linspace(axis[0], axis[-1], new_shape[d])
+            tables.append(_axis_table(axis, q, method))
+        idx = _device.to_device(np.concatenate([t[0] for t in tables]), torch.int32)
+        nearest = method == "nearest"
+        y = ym = None
+        if not nearest:
+            y = _device.to_device(np.concatenate([t[1] for t in tables]))
+            ym = _device.to_device(np.concatenate([t[2] for t in tables]))
+        v = self._device_grid().contiguous()
+        out = torch.empty(new_shape, dtype=torch.float64, device=v.device)
+        dims = np.ascontiguousarray(self.shape, dtype=np.int32)
+        odims = np.ascontiguousarray(new_shape, dtype=np.int32)
+        rc = _lib.load().fteik_resample(
+            nd, int(nearest), _device.ptr(v), _device.host_ptr(dims), _device.host_ptr(odims),
+            _device.ptr(idx), _device.ptr(y), _device.ptr(ym), _device.ptr(out),
+            _device.stream(),
+        )
+        _lib.check(rc, "resample")
+        old_shape = self.shape
+        self._grid = out
+        self._gridsize = tuple(a * b / c for a, b, c in zip(self.gridsize, old_shape, new_shape))
+
+    def _smooth_device(self, sigma):
+        """gaussian_filter(grid, sigma / gridsize) (fteikpy/_base.py:112-123,
+        201-212): one 1D correlation per axis whose sigma exceeds 1e-15, in
+        axis order, mode 'reflect', truncate 4, by ``fteik_correlate1d``."""
+        nd = self._ndim
+        sigma = np.full(nd, sigma) if np.ndim(sigma) == 0 else np.asarray(sigma)
+        sig = np.asarray(sigma, dtype=np.float64) / np.asarray(self._gridsize)
+        lib = _lib.load()
+        cur = self._device_grid().contiguous()
+        dims = np.ascontiguousarray(cur.shape, dtype=np.int32)
+        for d in range(nd):
+            if not sig[d] > 1e-15:
+                continue
+            w = _device.to_device(_gaussian_weights(sig[d]))
+            out = torch.empty_like(cur)
+            rc = lib.fteik_correlate1d(
+                nd, _device.ptr(cur), _device.host_ptr(dims), d, _device.ptr(w), w.numel(),
+                _device.ptr(out), _device.stream(),
+            )
+            _lib.check(rc, "smooth")
+            cur = out
+        self._grid = cur.clone() if cur is self._dev else cur
+
+
+class BaseGrid2D(BaseGrid, _GridOpsMixin):
     _ndim = 2
 
     def __call__(self, points, fill_value=np.nan):
@@ -144,31 +229,12 @@ class BaseGrid2D(BaseGrid):
         return self._interp_device(points, fill_value)
 
     def resample(self, new_shape, method="linear"):
-        """Resample grid (fteikpy/_base.py:81-110; model preparation, done with
-        SciPy on the host exactly as the reference does)."""
-        from scipy.interpolate import RegularGridInterpolator
-
-        zaxis = self.zaxis
-        xaxis = self.xaxis
-        Z, X = np.meshgrid(
-            np.linspace(zaxis[0], zaxis[-1], new_shape[0]),
-            np.linspace(xaxis[0], xaxis[-1], new_shape[1]),
-            indexing="ij",
-        )
-        fn = RegularGridInterpolator(
-            points=(zaxis, xaxis), values=self._grid, method=method, bounds_error=False
-        )
-        self._grid = fn([[z, x] for z, x in zip(Z.ravel(), X.ravel())]).reshape(new_shape)
-        self._gridsize = tuple(
-            a * b / c for a, b, c in zip(self.gridsize, self.shape, new_shape)
-        )
+        """Resample grid (fteikpy/_base.py:81-110), on the device."""
+        self._resample_device(new_shape, method)
 
     def smooth(self, sigma):
-        """Smooth grid (fteikpy/_base.py:112-123; SciPy on the host)."""
-        from scipy.ndimage import gaussian_filter
-
-        sigma = np.full(2, sigma) if np.ndim(sigma) == 0 else np.asarray(sigma)
-        self._grid = gaussian_filter(self._grid, sigma / self._gridsize)
+        """Smooth grid (fteikpy/_base.py:112-123), on the device."""
+        self._smooth_device(sigma)
 
     def _axes(self):
         return [self.zaxis, self.xaxis]
@@ -184,7 +250,7 @@ class BaseGrid2D(BaseGrid):
         return self._axis(1)
 
 
-class BaseGrid3D(BaseGrid):
+class BaseGrid3D(BaseGrid, _GridOpsMixin):
     _ndim = 3
 
     def __call__(self, points, fill_value=np.nan):
@@ -192,34 +258,12 @@ class BaseGrid3D(BaseGrid):
         return self._interp_device(points, fill_value)
 
     def resample(self, new_shape, method="linear"):
-        """Resample grid (fteikpy/_base.py:165-199; SciPy on the host)."""
-        from scipy.interpolate import RegularGridInterpolator
-
-        zaxis = self.zaxis
-        xaxis = self.xaxis
-        yaxis = self.yaxis
-        Z, X, Y = np.meshgrid(
-            np.linspace(zaxis[0], zaxis[-1], new_shape[0]),
-            np.linspace(xaxis[0], xaxis[-1], new_shape[1]),
-            np.linspace(yaxis[0], yaxis[-1], new_shape[2]),
-            indexing="ij",
-        )
-        fn = RegularGridInterpolator(
-            points=(zaxis, xaxis, yaxis), values=self._grid, method=method, bounds_error=False
-        )
-        self._grid = fn(
-            [[z, x, y] for z, x, y in zip(Z.ravel(), X.ravel(), Y.ravel())]
-        ).reshape(new_shape)
-        self._gridsize = tuple(
-            a * b / c for a, b, c in zip(self.gridsize, self.shape, new_shape)
-        )
+        """Resample grid (fteikpy/_base.py:165-199), on the device."""
+        self._resample_device(new_shape, method)
 
     def smooth(self, sigma):
-        """Smooth grid (fteikpy/_base.py:201-212; SciPy on the host)."""
-        from scipy.ndimage import gaussian_filter
-
-        sigma = np.full(3, sigma) if np.ndim(sigma) == 0 else np.asarray(sigma)
-        self._grid = gaussian_filter(self._grid, sigma / self._gridsize)
+        """Smooth grid (fteikpy/_base.py:201-212), on the device."""
+        self._smooth_device(sigma)
 
     def _axes(self):
         return [self.zaxis, self.xaxis, self.yaxis]

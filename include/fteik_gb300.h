@@ -204,6 +204,27 @@ int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, double dz, doubl
                     const double* grad_tt_rec, double* grad_slow, void* workspace,
                     size_t workspace_bytes, long long spin_limit, void* stream);
 
+/* ------------------------------------------------------ model preparation --
+ * Replace the SciPy calls of Grid*.resample / Grid*.smooth
+ * (fteikpy/_base.py:81-123, 165-212) with device kernels.
+ *
+ * fteik_resample: RegularGridInterpolator (linear or, with nearest != 0,
+ * nearest) at a tensor grid of query points. values: device [dims] (C order,
+ * nd = 2 or 3); out: device [out_dims]. The per-axis tables, concatenated
+ * axis by axis (out_dims[0] entries, then out_dims[1], ...), are device
+ * arrays: idx the lower node index (nearest: the node), y the normalised
+ * distance in the cell and ym = 1 - y (both unused for nearest). The corner
+ * sum follows scipy's _evaluate_linear order.
+ *
+ * fteik_correlate1d: out = in correlated with `weights` (device, odd count,
+ * centred) along `axis`, mode 'reflect' (scipy.ndimage.correlate1d with
+ * origin 0); gaussian_filter is one call per axis. in and out must differ. */
+int fteik_resample(int nd, int nearest, const double* values, const int* dims,
+                   const int* out_dims, const int* idx, const double* y, const double* ym,
+                   double* out, void* stream);
+int fteik_correlate1d(int nd, const double* in, const int* dims, int axis,
+                      const double* weights, int nweights, double* out, void* stream);
+
 /* ---------------------------------------------------------------- 2D solve --
  * Replaces solve2d / fteik2d / fteik2d_vectorized
  * (fteikpy/_fteik/_fteik2d.py:290-674) as called by Eikonal2D.solve

@@ -127,20 +127,47 @@ def test_api_host_logic():
         tt2.gradient
 
 
-def test_resample_and_smooth_match_reference_semantics():
-    # fteikpy tests/test_eikonal3d.py:48-60 and test_eikonal2d.py:36-48
-    eik = fp.Eikonal3D(np.ones((16, 16, 16)), (1.0, 1.0, 1.0))
-    eik.resample((32, 32, 32))
-    assert eik.grid.sum() == 16 * 16 * 16 * 8.0
-    eik = fp.Eikonal3D(np.ones((16, 16, 16)), (1.0, 1.0, 1.0))
-    eik.smooth(1.0)
-    assert eik.grid.sum() == eik.grid.size
-    eik2 = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
-    eik2.resample((32, 32))
-    assert eik2.grid.sum() == 16 * 16 * 4.0
-    eik2 = fp.Eikonal2D(np.ones((16, 16)), (1.0, 1.0))
-    eik2.smooth(1.0)
-    assert eik2.grid.sum() == eik2.grid.size
+def test_grid_ops_host_checks(lib):
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    d3 = np.ascontiguousarray([4, 5, 6], dtype=np.int32)
+    bad = np.ascontiguousarray([4, 0, 6], dtype=np.int32)
+    one = np.ascontiguousarray([1, 5, 6], dtype=np.int32)
+    INV = _lib.INVALID_ARGUMENT
+    # no GPU needed: every call below fails its host-side checks first
+    assert lib.fteik_resample(0, 0, FAKE, p(d3), p(d3), FAKE, FAKE, FAKE, FAKE, None) == INV
+    assert lib.fteik_resample(3, 0, FAKE, p(bad), p(d3), FAKE, FAKE, FAKE, FAKE, None) == INV
+    assert lib.fteik_resample(3, 0, FAKE, p(one), p(d3), FAKE, FAKE, FAKE, FAKE, None) == INV
+    assert lib.fteik_resample(3, 0, FAKE, p(d3), p(d3), FAKE, None, FAKE, FAKE, None) == INV
+    w = ctypes.c_void_p(0x2000)
+    assert lib.fteik_correlate1d(3, FAKE, p(d3), 3, w, 5, w, None) == INV
+    assert lib.fteik_correlate1d(3, FAKE, p(d3), 0, w, 4, w, None) == INV
+    assert lib.fteik_correlate1d(3, FAKE, p(d3), 0, w, 5, FAKE, None) == INV  # in place
+
+
+def test_grid_op_tables_follow_scipy():
+    """The host half of resample/smooth: per-axis lookups and Gaussian
+    weights, checked against SciPy (the device half runs in the GPU tests)."""
+    from scipy.interpolate import RegularGridInterpolator
+    from scipy.ndimage import gaussian_filter1d
+
+    from fteikpy_gb300._base import _axis_table, _gaussian_weights
+
+    axis = 3.0 + 7.5 * np.arange(11)
+    q = np.linspace(axis[0], axis[-1], 29)
+    i, y, ym = _axis_table(axis, q, "linear")
+    vals = np.random.default_rng(0).uniform(1, 2, 11)
+    lin = vals[i] * ym + vals[i + 1] * y
+    ref = RegularGridInterpolator((axis,), vals)(q[:, None])
+    assert np.allclose(lin, ref, rtol=1e-15, atol=0)
+    near, _, _ = _axis_table(axis, q, "nearest")
+    ref = RegularGridInterpolator((axis,), vals, method="nearest")(q[:, None])
+    assert np.array_equal(vals[near], ref)
+    for sigma in (0.3, 1.0, 2.7):
+        w = _gaussian_weights(sigma)
+        x = np.zeros(4 * len(w) + 1)
+        x[len(x) // 2] = 1.0
+        assert np.allclose(gaussian_filter1d(x, sigma)[len(x) // 2 - len(w) // 2:][:len(w)],
+                           w[::-1], rtol=1e-14, atol=1e-17)
 
 
 def _batch_args(dims, nsrc, sources, spacing=None):

@@ -190,7 +190,10 @@ __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double
 // _fteik3d.py:149-158); computed in double precision each lies within
 // 2^-46 * M of that bound, M the largest input.  So if every 1D candidate is
 // >= t0 and every diagonal input is >= t0 + 2^-43 * M, no operator can beat
-// t0 (the minimum keeps t0 on ties) and the update is skipped.
+// t0 (the minimum keeps t0 on ties) and the update is skipped.  (Also
+// accepting nodes whose plane guards fail would catch more of them, but the
+// guards' coefficient reads then run for every node and cost more than the
+// extra skips save.)
 __device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, double t1d3,
                                          double tv, double te, double tn, double tev, double ten,
                                          double tnv, double tnve) {
@@ -781,11 +784,20 @@ static void tuned_store(const std::vector<long long>& key, const Tune3& t) {
   g_tuned[key] = t;
 }
 
+// Default shape for `jobs` (model, source) pairs in flight, of which
+// `coef_sources` share one model's coefficients: with few jobs the solve is
+// bound by the latency of the pencil wavefront, and publishing progress
+// every step (chunk 1) lets downwind pencils start soonest; with many, the
+// FP64 pipe is the bound and fewer publications cost less.
+static Tune3 default_tune(int jobs, int coef_sources) {
+  const int chunk = jobs <= 2 ? 1 : jobs <= 8 ? 2 : kDefaultChunk;
+  return Tune3{kDefaultPencil, chunk, coef_sources >= kCoefMinSources ? 1 : 0};
+}
+
 // The shape a solve runs with: explicit options first, then a shape the
-// autotuner measured for this signature, then the defaults (coefficient
-// arrays once `coef_sources` sources share them).
-static Tune3 resolve_tune(const std::vector<long long>& key, int coef_sources) {
-  Tune3 t{kDefaultPencil, kDefaultChunk, coef_sources >= kCoefMinSources ? 1 : 0};
+// autotuner measured for this signature, then the defaults.
+static Tune3 resolve_tune(const std::vector<long long>& key, int jobs, int coef_sources) {
+  Tune3 t = default_tune(jobs, coef_sources);
   Tune3 m;
   if (tuned_lookup(key, &m)) t = m;
   const long long op = option_value(kOptSweepPencil), oc = option_value(kOptSweepChunk),
@@ -853,7 +865,8 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
                     (0.0 <= y && y <= dy * ny);
     if (!ok) return kSourceOutOfBound;
   }
-  const Tune3 tune = force ? *force : resolve_tune(single_key(nz, nx, ny, nsrc, grad), nsrc);
+  const Tune3 tune =
+      force ? *force : resolve_tune(single_key(nz, nx, ny, nsrc, grad), nsrc, nsrc);
   const int pw = tune.pencil, pk = 32 / pw;
   const int NZ = nz + 1, NX = nx + 1, NY = ny + 1;
   const int PJ = (NX + pw - 1) / pw, PK = (NY + pk - 1) / pk;
@@ -1086,8 +1099,9 @@ static int solve_batch_impl(int nmodel, const double* const* slow, const int* di
   }
   const Batch3Layout L = batch_layout(nmodel, dims, nsrc, grad);
   if (workspace_bytes < L.total) return kWorkspaceTooSmall;
-  const Tune3 tune = force ? *force : resolve_tune(batch_key(nmodel, dims, nsrc, grad),
-                                                   (int)(total_src / nmodel));
+  const Tune3 tune = force ? *force
+                          : resolve_tune(batch_key(nmodel, dims, nsrc, grad), (int)total_src,
+                                         (int)(total_src / nmodel));
   const int pw = tune.pencil, pk = 32 / pw;
   char* ws = (char*)workspace;
 
@@ -1229,8 +1243,8 @@ namespace {
 // coefficient source, each timed (sweep kernel only, CUDA events on the
 // stream) with one sweep per direction, the best of `reps` runs.
 template <class Run>
-int tune_search(Run run, int coef_sources, int reps, Tune3* best, float* best_ms) {
-  Tune3 cur{kDefaultPencil, kDefaultChunk, coef_sources >= kCoefMinSources ? 1 : 0};
+int tune_search(Run run, int jobs, int coef_sources, int reps, Tune3* best, float* best_ms) {
+  Tune3 cur = default_tune(jobs, coef_sources);
   float cur_ms = 0.f;
   auto time_of = [&](const Tune3& t, float* ms) -> int {
     float b = 3.4e38f;
@@ -1304,7 +1318,7 @@ extern "C" int fteik3d_autotune(const double* slow, int nz, int nx, int ny, doub
   Tune3 best;
   float ms = 0.f;
   const bool timing_was_on = kernel_timing_on();
-  const int rc = tune_search(run, nsrc, 2, &best, &ms);
+  const int rc = tune_search(run, nsrc, nsrc, 2, &best, &ms);
   fteik_kernel_timing(timing_was_on ? 1 : 0);
   if (rc != kOk) return rc;
   tuned_store(single_key(nz, nx, ny, nsrc, grad), best);
@@ -1338,7 +1352,7 @@ extern "C" int fteik3d_batch_autotune(int nmodel, const double* const* slow, con
   Tune3 best;
   float ms = 0.f;
   const bool timing_was_on = kernel_timing_on();
-  const int rc = tune_search(run, (int)(total / nmodel), 1, &best, &ms);
+  const int rc = tune_search(run, (int)total, (int)(total / nmodel), 1, &best, &ms);
   fteik_kernel_timing(timing_was_on ? 1 : 0);
   if (rc != kOk) return rc;
   tuned_store(batch_key(nmodel, dims, nsrc, grad), best);

@@ -274,12 +274,14 @@ def autotune(solvers, sources, return_gradient=False):
 
     ``solvers`` is one Eikonal3D (``sources`` as its ``solve`` takes them) or a
     list of them (``sources`` a list, as ``solve_batch`` takes them). Returns
-    {"pencil": w, "chunk": c, "coef": f, "ms": t}: pencil width along x, steps
-    between progress publications, coefficient source (1 arrays, 0 cells), and
-    the sweep kernel's time for one sweep per direction.
+    {"pencil": w, "chunk": c, "coef": f, "team": m, "ms": t}: pencil width
+    along x, steps between progress publications, coefficient source (1
+    arrays, 0 cells), whether blocks of 4 sources step together with
+    compacted operators, and the sweep kernel's time for one sweep per
+    direction.
     """
     lib = _lib.load()
-    shape = (ctypes.c_int * 3)()
+    shape = (ctypes.c_int * 4)()
     ms = ctypes.c_float()
     if isinstance(solvers, Eikonal3D):
         src = np.ascontiguousarray(np.atleast_2d(solvers._prepare_sources(sources)[1]))
@@ -307,4 +309,5 @@ def autotune(solvers, sources, return_gradient=False):
             shape, ctypes.byref(ms), _device.stream(),
         )
     _lib.check(rc, "autotune")
-    return {"pencil": shape[0], "chunk": shape[1], "coef": shape[2], "ms": float(ms.value)}
+    return {"pencil": shape[0], "chunk": shape[1], "coef": shape[2], "team": shape[3],
+            "ms": float(ms.value)}

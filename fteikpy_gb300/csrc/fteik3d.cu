@@ -109,57 +109,54 @@ struct CoefCells {
 
 // One node update, _fteik3d.py:38-200, with the slowness-only factors taken
 // from the coefficient provider c (see Coef3 for which factor is which).
-// Takes the three 1D candidates (_fteik3d.py:76-104: t1d1 = tv + c.z1() ...),
-// which the caller computes first to test whether the node can change.
-template <bool GRAD, class CP>
-__device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
-                                                double te, double tn, double tev, double ten,
-                                                double tnv, double tnve, double t0,
-                                                const CP& c, const Ops3& o, int sz, int sx,
-                                                int sy, uint8_t& code) {
+// Plane operator of plane P (0 ZX, 1 ZY, 2 XY, _fteik3d.py:106-143) on its
+// inputs (u, w, x) = (tv, te, tev), (tv, tn, tnv) or (te, tn, ten), for a node
+// whose guard holds; q4 = 4 v^2 (sum of the plane's two inverse squares).
+// The reference forms ta = tev + te - tv, tb = tev - te + tv for ZX and
+// ta = u - w + x, tb = w - u + x for ZY and XY; both are written as
+// (p1 + p2) + p3 with negated operands (x - y is x + (-y) exactly), so one
+// instruction sequence serves every plane when P differs between lanes.
+__device__ __forceinline__ double plane3(int P, double u, double w, double x, double q4,
+                                         const Ops3& o) {
+  const bool zx = P == 0;
+  // operands picked first, so that each sum is one add sequence for any P
+  const double a1 = zx ? x : u, a2 = zx ? w : -w, a3 = zx ? -u : x;
+  const double b1 = zx ? x : w, b2 = zx ? -w : -u, b3 = zx ? u : x;
+  const double ta = (a1 + a2) + a3;
+  const double tb = (b1 + b2) + b3;
+  const double p = zx ? tb : ta, q = zx ? ta : tb;
+  const double cp = P == 2 ? o.dx2i : o.dz2i;
+  const double cq = P == 0 ? o.dx2i : o.dy2i;
+  const double prod = P == 0 ? o.dz2dx2 : P == 1 ? o.dz2dy2 : o.dx2dy2;
+  const Recip& r = P == 0 ? o.rzx : P == 1 ? o.rzy : o.rxy;
+  return plane_op(p, cp, q, cq, ta - tb, q4, prod, r);
+}
+
+// 3D operator, _fteik3d.py:145-159, for a node whose guard
+// max(tv, te, tn) < min(t1d, t2d) holds; t2 = s^2 * dsum * 9.
+__device__ __forceinline__ double op3d(double tv, double te, double tn, double tev, double ten,
+                                       double tnv, double tnve, double t2, const Ops3& o) {
+  const double htn = half(tn), hten = half(ten), htv = half(tv), htev = half(tev);
+  const double htnv = half(tnv), hte = half(te);
+  double ta = te - htn + hten - htv + htev - tnv + tnve;
+  double tb = tv - htn + htnv - hte + htev - ten + tnve;
+  double tc = tn - hte + hten - htv + htnv - tev + tnve;
+  double dab = ta - tb, dbc = tb - tc, dac = ta - tc;
+  double t3 = o.dz2dx2 * (dab * dab);
+  t3 += o.dz2dy2 * (dbc * dbc);
+  t3 += o.dx2dy2 * (dac * dac);
+  if (!dle(t3, t2)) return kBig;
+  double t1 = tb * o.dz2i + ta * o.dx2i + tc * o.dy2i;
+  return div_by(t1 + sqrt(t2 - t3), o.rsum);
+}
+
+// Minimum with the old value and the branch record, _fteik3d.py:161-200.
+template <bool GRAD>
+__device__ __forceinline__ double finish3d(double t0, double t1d1, double t1d2, double t1d3,
+                                           double t2d1, double t2d2, double t2d3, double t3d,
+                                           int sz, int sx, int sy, uint8_t& code) {
   const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
-
-  // 2D operators, _fteik3d.py:106-143
-  double t2d1 = kBig;
-  if (dlt(tv, te + c.zxa()) && dlt(te, tv + c.zxb())) {
-    double ta = tev + te - tv;
-    double tb = tev - te + tv;
-    t2d1 = plane_op(tb, o.dz2i, ta, o.dx2i, ta - tb, c.zxq(), o.dz2dx2, o.rzx);
-  }
-  double t2d2 = kBig;
-  if (dlt(tv, tn + c.zya()) && dlt(tn, tv + c.zyb())) {
-    double ta = tv - tn + tnv;
-    double tb = tn - tv + tnv;
-    t2d2 = plane_op(ta, o.dz2i, tb, o.dy2i, ta - tb, c.zyq(), o.dz2dy2, o.rzy);
-  }
-  double t2d3 = kBig;
-  if (dlt(te, tn + c.xya()) && dlt(tn, te + c.xyb())) {
-    double ta = te - tn + ten;
-    double tb = tn - te + ten;
-    t2d3 = plane_op(ta, o.dx2i, tb, o.dy2i, ta - tb, c.xyq(), o.dx2dy2, o.rxy);
-  }
   const double t2d = dmin(dmin(t2d1, t2d2), t2d3);
-
-  // 3D operator, _fteik3d.py:145-159
-  double t3d = kBig;
-  if (dlt(dmax(dmax(tv, te), tn), dmin(t1d, t2d))) {
-    const double htn = half(tn), hten = half(ten), htv = half(tv), htev = half(tev);
-    const double htnv = half(tnv), hte = half(te);
-    double ta = te - htn + hten - htv + htev - tnv + tnve;
-    double tb = tv - htn + htnv - hte + htev - ten + tnve;
-    double tc = tn - hte + hten - htv + htnv - tev + tnve;
-    double t2 = c.t3();
-    double dab = ta - tb, dbc = tb - tc, dac = ta - tc;
-    double t3 = o.dz2dx2 * (dab * dab);
-    t3 += o.dz2dy2 * (dbc * dbc);
-    t3 += o.dx2dy2 * (dac * dac);
-    if (dle(t3, t2)) {
-      double t1 = tb * o.dz2i + ta * o.dx2i + tc * o.dy2i;
-      t3d = div_by(t1 + sqrt(t2 - t3), o.rsum);
-    }
-  }
-
-  // _fteik3d.py:161-200
   const double tnew = dmin(dmin(dmin(t0, t1d), t2d), t3d);
   if (GRAD && !deq(tnew, t0)) {
     int a, b, c;
@@ -181,6 +178,27 @@ __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double
     code = (uint8_t)((a + 1) * 9 + (b + 1) * 3 + (c + 1));
   }
   return tnew;
+}
+
+// One node update, _fteik3d.py:38-200.  Takes the three 1D candidates
+// (_fteik3d.py:76-104: t1d1 = tv + c.z1() ...), which the caller computes
+// first to test whether the node can change.
+template <bool GRAD, class CP>
+__device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
+                                                double te, double tn, double tev, double ten,
+                                                double tnv, double tnve, double t0,
+                                                const CP& c, const Ops3& o, int sz, int sx,
+                                                int sy, uint8_t& code) {
+  const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
+  double t2d1 = kBig, t2d2 = kBig, t2d3 = kBig;
+  if (dlt(tv, te + c.zxa()) && dlt(te, tv + c.zxb())) t2d1 = plane3(0, tv, te, tev, c.zxq(), o);
+  if (dlt(tv, tn + c.zya()) && dlt(tn, tv + c.zyb())) t2d2 = plane3(1, tv, tn, tnv, c.zyq(), o);
+  if (dlt(te, tn + c.xya()) && dlt(tn, te + c.xyb())) t2d3 = plane3(2, te, tn, ten, c.xyq(), o);
+  const double t2d = dmin(dmin(t2d1, t2d2), t2d3);
+  double t3d = kBig;
+  if (dlt(dmax(dmax(tv, te), tn), dmin(t1d, t2d)))
+    t3d = op3d(tv, te, tn, tev, ten, tnv, tnve, c.t3(), o);
+  return finish3d<GRAD>(t0, t1d1, t1d2, t1d3, t2d1, t2d2, t2d3, t3d, sz, sx, sy, code);
 }
 
 // True when the node provably keeps t0 in this sweep, on a grid with equal
@@ -256,6 +274,7 @@ struct Sweep3Args {
   const Job3* jobs;
   const int2* items;  // (job, JL << 16 | KL), by diagonal, then job
   unsigned items_per_epoch;
+  int ngroups;        // team kernel: groups of kTeamWarps sources
   // both
   unsigned* ticket;
   int* status;
@@ -529,6 +548,324 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
   }
 }
 
+// ------------------------------------------------------------- team kernel --
+//
+// The same sweeps for batches of sources, with the operators compacted.  In
+// the warp-per-pencil kernel above every 2D and 3D operator runs as a full
+// warp instruction even when few lanes need it: a plane operator's guard
+// holds in about half the lanes that update, the 3D operator's in a sixth,
+// and unchanged nodes (keeps_t0) idle in warps that still run.  Here a block
+// of kTeamWarps warps takes one pencil of one sweep for kTeamWarps sources
+// (warp w: source group * kTeamWarps + w) and steps them together.  Per step:
+//   A  each lane reads its inputs (as above), forms the 1D candidates and the
+//      plane guards, and queues one job per plane whose guard holds;
+//   B  the block evaluates the queued plane operators 32 to a warp instruction;
+//   C  each lane takes its plane results, tests the 3D guard and queues a job;
+//   D  the block evaluates the queued 3D operators;
+//   E  each lane forms the minimum and the branch record and writes back.
+// (Evaluating the rare 3D operator in place, or queueing it before the plane
+// results are known, saves two barriers per step but measured slower.)
+// Operators and their operands are the same as in node_update3d, so results
+// are bit-identical; only which lane evaluates an operator changes.
+constexpr int kTeamWarps = 4;
+// Resident team blocks per SM the registers are budgeted for.
+#ifndef FTEIK_TEAM_MIN_BLOCKS
+#define FTEIK_TEAM_MIN_BLOCKS 7
+#endif
+
+struct TeamShared {
+  // plane jobs, warp w's in [w][0, n2[w]): plane, lane and inputs (u, w, x, q4)
+  double ju[kTeamWarps][96], jw[kTeamWarps][96], jx[kTeamWarps][96], jq[kTeamWarps][96];
+  int jid[kTeamWarps][96];  // plane * 32 + lane
+  double r2[kTeamWarps][3][32];
+  // 3D jobs: lane and inputs (tv, te, tn, tev, ten, tnv, tnve, t2)
+  double kin[8][kTeamWarps][32];
+  int kid[kTeamWarps][32];
+  double r3[kTeamWarps][32];
+  int n2[kTeamWarps], n3[kTeamWarps];
+  unsigned ticket;
+};
+
+template <bool GRAD, bool COEF, int PW>
+__global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
+    sweep3d_team_kernel(const __grid_constant__ Sweep3Args A) {
+  constexpr int PJW = PW, PKW = 32 / PW, LAG = PJW + PKW - 2;
+  __shared__ TeamShared sh;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lj = lane / PKW, lk = lane % PKW;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const unsigned per_epoch = (unsigned)A.npencils * A.ngroups;
+  const unsigned total_items = (unsigned)A.nepochs * per_epoch;
+  const unsigned cmask = (unsigned)A.chunk - 1u;
+  const Ops3& o = A.o;
+  const long long NXY = (long long)A.NX * A.NY;
+  const int T = A.total_steps;
+
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) sh.ticket = atomicAdd(A.ticket, 1u);
+    __syncthreads();
+    const unsigned t = sh.ticket;
+    if (t >= total_items) break;
+    const int e = (int)(t / per_epoch);
+    const unsigned rem = t - (unsigned)e * per_epoch;
+    const int p = (int)(rem / A.ngroups);
+    const int src = (int)(rem - (unsigned)p * A.ngroups) * kTeamWarps + warp;
+    bool active = src < A.nsrc;
+    const int dir = e & 7;
+    const int sz = dir < 4 ? 1 : -1, sx = (dir & 1) ? -1 : 1, sy = (dir & 2) ? -1 : 1;
+    const int JL = A.order[p] >> 16, KL = A.order[p] & 0xffff;
+    const int J = sx > 0 ? JL : A.PJ - 1 - JL;
+    const int K = sy > 0 ? KL : A.PK - 1 - KL;
+    const int src_c = active ? src : 0;
+    unsigned* prog = A.progress + (long long)src_c * A.npencils;
+    unsigned* my_prog = prog + J * A.PK + K;
+    const unsigned base = (unsigned)e * A.stride;
+
+    // Dependencies on the previous sweep (see sweep3d_kernel).
+    if (active) {
+      bool ok = true;
+      if (lane == 0 && e > 0) {
+        const int pd = (e - 1) & 7;
+        const int psx = (pd & 1) ? -1 : 1, psy = (pd & 2) ? -1 : 1;
+        const unsigned done = base - A.stride + (unsigned)T;
+        ok = wait_geq(my_prog, done, A.status, A.spin_limit);
+        const int J2 = J + psx, K2 = K + psy;
+        const bool hj = J2 >= 0 && J2 < A.PJ, hk = K2 >= 0 && K2 < A.PK;
+        if (ok && hj) ok = wait_geq(prog + J2 * A.PK + K, done, A.status, A.spin_limit);
+        if (ok && hk) ok = wait_geq(prog + J * A.PK + K2, done, A.status, A.spin_limit);
+        if (ok && hj && hk) ok = wait_geq(prog + J2 * A.PK + K2, done, A.status, A.spin_limit);
+      }
+      active = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    }
+
+    const int Ju = J - sx, Ku = K - sy;
+    const bool hJu = Ju >= 0 && Ju < A.PJ, hKu = Ku >= 0 && Ku < A.PK;
+    const unsigned* prog_j = prog + Ju * A.PK + K;
+    const unsigned* prog_k = prog + J * A.PK + Ku;
+    const unsigned* prog_jk = prog + Ju * A.PK + Ku;
+    const int j = sx > 0 ? J * PJW + lj : J * PJW + (PJW - 1) - lj;
+    const int k = sy > 0 ? K * PKW + lk : K * PKW + (PKW - 1) - lk;
+    const bool in_grid = j < A.NX && k < A.NY;
+    const bool frozen_jk = (j == (sx > 0 ? 0 : A.NX - 1)) || (k == (sy > 0 ? 0 : A.NY - 1));
+    const int j1 = sx > 0 ? j - 1 : j, k1 = sy > 0 ? k - 1 : k;
+    const long long jk = (long long)j * A.NY + k;
+    const long long j1k = (long long)j1 * A.NY + k, jk1 = (long long)j * A.NY + k1;
+    const long long j1k1 = (long long)j1 * A.NY + k1;
+    const int jm = imax(j - 1, 0), jp = imin(j, A.NX - 2);
+    const int km = imax(k - 1, 0), kp = imin(k, A.NY - 2);
+    const long long NYc = A.ny, NXYc = (long long)A.nx * A.ny;
+    const long long ju = (sx > 0 ? jm : jp) * NYc, jo = (sx > 0 ? jp : jm) * NYc;
+    const long long ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
+    double* tts = A.tt + (long long)src_c * A.nodes;
+    uint8_t* recs = GRAD ? A.rec + (long long)src_c * A.nodes : nullptr;
+    const long long dj = (long long)sx * A.NY, dk = sy;
+    const long long di = (long long)sz * NXY;
+    const bool may_skip = *A.no_skip == 0;
+    const long long big_bits = __double_as_longlong(kBig);
+
+    double r1 = 0.0, r2v = 0.0, r3v = 0.0;
+    for (int s = 0; s < T; ++s) {
+      if (active && ((unsigned)s & cmask) == 0) {
+        const int last = imin(s + (int)cmask, T - 1);
+        bool w = true;
+        if (lane == 0) {
+          if (hJu) w = wait_geq(prog_j, base + (unsigned)imin(last + PJW, T), A.status, A.spin_limit);
+          if (w && hKu)
+            w = wait_geq(prog_k, base + (unsigned)imin(last + PKW, T), A.status, A.spin_limit);
+          if (w && hJu && hKu)
+            w = wait_geq(prog_jk, base + (unsigned)imin(last + LAG + 1, T), A.status,
+                         A.spin_limit);
+          if (w) __threadfence();
+        }
+        active = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
+      }
+      // ---- stage A: inputs, 1D candidates, guards, plane jobs ----
+      const double uj_1 = __shfl_up_sync(0xffffffffu, r1, PKW);
+      const double uj_2 = __shfl_up_sync(0xffffffffu, r2v, PKW);
+      const double uk_1 = __shfl_up_sync(0xffffffffu, r1, 1);
+      const double uk_2 = __shfl_up_sync(0xffffffffu, r2v, 1);
+      const double ujk_2 = __shfl_up_sync(0xffffffffu, r2v, PKW + 1);
+      const double ujk_3 = __shfl_up_sync(0xffffffffu, r3v, PKW + 1);
+      const int r = s - lj - lk;
+      const bool act = active && in_grid && r >= 0 && r < A.NZ;
+      const int i = sz > 0 ? r : A.NZ - 1 - r;
+      const long long n = (long long)i * NXY + jk;
+      const double t0 = act ? ld_cg(tts + n) : 0.0;
+      double res = t0;
+      bool go = act && r != 0 && !frozen_jk;
+      double tv = 0.0, te = 0.0, tn = 0.0, tev = 0.0, tnv = 0.0, ten = 0.0, tnve = 0.0;
+      double t1d1 = kBig, t1d2 = kBig, t1d3 = kBig;
+      bool czx = false, czy = false, cxy = false;
+      const long long i0 = (long long)i * NXY;
+      const long long i1 = (long long)(sz > 0 ? i - 1 : i) * NXY;
+      const CoefArrays ca{A.C,      i1 + jk,  i0 + j1k,  i0 + jk1,
+                          i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
+      CoefCells cc{{}, o};
+      double q_zx = 0.0, q_zy = 0.0, q_xy = 0.0;
+      if (go) {
+        tv = r1;
+        te = lj > 0 ? uj_1 : ld_cg(tts + n - dj);
+        tn = lk > 0 ? uk_1 : ld_cg(tts + n - dk);
+        tev = lj > 0 ? uj_2 : ld_cg(tts + n - di - dj);
+        tnv = lk > 0 ? uk_2 : ld_cg(tts + n - di - dk);
+        ten = (lj > 0 && lk > 0) ? ujk_2 : ld_cg(tts + n - dj - dk);
+        tnve = (lj > 0 && lk > 0) ? ujk_3 : ld_cg(tts + n - di - dj - dk);
+        if (may_skip) {
+          const long long b = __double_as_longlong(t0);
+          go = !(b == big_bits && __double_as_longlong(tv) == b &&
+                 __double_as_longlong(te) == b && __double_as_longlong(tn) == b &&
+                 __double_as_longlong(tev) == b && __double_as_longlong(tnv) == b &&
+                 __double_as_longlong(ten) == b && __double_as_longlong(tnve) == b);
+        }
+      }
+      if (go) {
+        if (COEF) {
+          t1d1 = tv + ca.z1();
+          t1d2 = te + ca.x1();
+          t1d3 = tn + ca.y1();
+        } else {
+          const int im = imax(i - 1, 0), ip = imin(i, A.NZ - 2);
+          const long long iu = (sz > 0 ? im : ip) * NXYc, io = (sz > 0 ? ip : im) * NXYc;
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+              for (int c = 0; c < 2; ++c)
+                cc.U[a][b][c] = __ldg(A.slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
+          t1d1 = tv + cc.z1();
+          t1d2 = te + cc.x1();
+          t1d3 = tn + cc.y1();
+        }
+        if (A.keep_test) go = !keeps_t0(t0, t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve);
+      }
+      if (go) {
+        if (COEF) {
+          czx = dlt(tv, te + ca.zxa()) && dlt(te, tv + ca.zxb());
+          czy = dlt(tv, tn + ca.zya()) && dlt(tn, tv + ca.zyb());
+          cxy = dlt(te, tn + ca.xya()) && dlt(tn, te + ca.xyb());
+          if (czx) q_zx = ca.zxq();
+          if (czy) q_zy = ca.zyq();
+          if (cxy) q_xy = ca.xyq();
+        } else {
+          czx = dlt(tv, te + cc.zxa()) && dlt(te, tv + cc.zxb());
+          czy = dlt(tv, tn + cc.zya()) && dlt(tn, tv + cc.zyb());
+          cxy = dlt(te, tn + cc.xya()) && dlt(tn, te + cc.xyb());
+          if (czx) q_zx = cc.zxq();
+          if (czy) q_zy = cc.zyq();
+          if (cxy) q_xy = cc.xyq();
+        }
+      }
+      {
+        const unsigned m0 = __ballot_sync(0xffffffffu, czx);
+        const unsigned m1 = __ballot_sync(0xffffffffu, czy);
+        const unsigned m2 = __ballot_sync(0xffffffffu, cxy);
+        const int b1 = __popc(m0), b2 = b1 + __popc(m1);
+        if (czx) {
+          const int q = __popc(m0 & lt_mask);
+          sh.ju[warp][q] = tv; sh.jw[warp][q] = te; sh.jx[warp][q] = tev; sh.jq[warp][q] = q_zx;
+          sh.jid[warp][q] = lane;
+        }
+        if (czy) {
+          const int q = b1 + __popc(m1 & lt_mask);
+          sh.ju[warp][q] = tv; sh.jw[warp][q] = tn; sh.jx[warp][q] = tnv; sh.jq[warp][q] = q_zy;
+          sh.jid[warp][q] = 32 + lane;
+        }
+        if (cxy) {
+          const int q = b2 + __popc(m2 & lt_mask);
+          sh.ju[warp][q] = te; sh.jw[warp][q] = tn; sh.jx[warp][q] = ten; sh.jq[warp][q] = q_xy;
+          sh.jid[warp][q] = 64 + lane;
+        }
+        if (lane == 0) sh.n2[warp] = b2 + __popc(m2);
+      }
+      __syncthreads();
+      // ---- stage B: the queued plane operators, 32 jobs per warp instruction ----
+      {
+        const int c0 = sh.n2[0], c1 = c0 + sh.n2[1], c2 = c1 + sh.n2[2], c3 = c2 + sh.n2[3];
+        for (int q = warp * 32 + lane; q - lane < c3; q += kTeamWarps * 32) {
+          if (q < c3) {
+            const int w = q < c0 ? 0 : q < c1 ? 1 : q < c2 ? 2 : 3;
+            const int l = q - (w == 0 ? 0 : w == 1 ? c0 : w == 2 ? c1 : c2);
+            const int id = sh.jid[w][l];
+            sh.r2[w][id >> 5][id & 31] =
+                plane3(id >> 5, sh.ju[w][l], sh.jw[w][l], sh.jx[w][l], sh.jq[w][l], o);
+          }
+        }
+      }
+      __syncthreads();
+      // ---- stage C: plane results, 3D guard, 3D jobs ----
+      const double t2d1 = czx ? sh.r2[warp][0][lane] : kBig;
+      const double t2d2 = czy ? sh.r2[warp][1][lane] : kBig;
+      const double t2d3 = cxy ? sh.r2[warp][2][lane] : kBig;
+      const bool g3 = go && dlt(dmax(dmax(tv, te), tn),
+                                dmin(dmin(dmin(t1d1, t1d2), t1d3), dmin(dmin(t2d1, t2d2), t2d3)));
+      {
+        const unsigned m3 = __ballot_sync(0xffffffffu, g3);
+        if (g3) {
+          const int q = __popc(m3 & lt_mask);
+          sh.kin[0][warp][q] = tv;
+          sh.kin[1][warp][q] = te;
+          sh.kin[2][warp][q] = tn;
+          sh.kin[3][warp][q] = tev;
+          sh.kin[4][warp][q] = ten;
+          sh.kin[5][warp][q] = tnv;
+          sh.kin[6][warp][q] = tnve;
+          sh.kin[7][warp][q] = COEF ? ca.t3() : cc.t3();
+          sh.kid[warp][q] = lane;
+        }
+        if (lane == 0) sh.n3[warp] = __popc(m3);
+      }
+      __syncthreads();
+      // ---- stage D: 3D operators ----
+      {
+        const int c0 = sh.n3[0], c1 = c0 + sh.n3[1], c2 = c1 + sh.n3[2], c3 = c2 + sh.n3[3];
+        for (int q = warp * 32 + lane; q - lane < c3; q += kTeamWarps * 32) {
+          if (q < c3) {
+            const int w = q < c0 ? 0 : q < c1 ? 1 : q < c2 ? 2 : 3;
+            const int l = q - (w == 0 ? 0 : w == 1 ? c0 : w == 2 ? c1 : c2);
+            sh.r3[w][sh.kid[w][l]] =
+                op3d(sh.kin[0][w][l], sh.kin[1][w][l], sh.kin[2][w][l], sh.kin[3][w][l],
+                     sh.kin[4][w][l], sh.kin[5][w][l], sh.kin[6][w][l], sh.kin[7][w][l], o);
+          }
+        }
+      }
+      __syncthreads();
+      // ---- stage E: minimum, branch record, write-back ----
+      if (go) {
+        const double t3d = g3 ? sh.r3[warp][lane] : kBig;
+        uint8_t code = 0;
+        res = finish3d<GRAD>(t0, t1d1, t1d2, t1d3, t2d1, t2d2, t2d3, t3d, sz, sx, sy, code);
+        if (!deq(res, t0)) {
+          tts[n] = res;
+          if (GRAD) recs[n] = code;
+          if (A.tape_code) {
+            const long long tq = ((long long)e * A.nsrc + src) * A.nodes + n;
+            A.tape_code[tq] = code;
+            A.tape_old[tq] = t0;
+          }
+        }
+      }
+      r3v = r2v;
+      r2v = r1;
+      r1 = res;
+      if (active && (((unsigned)(s + 1) & cmask) == 0 || s + 1 == T)) {
+        __syncwarp();
+        if (lane == 0) {
+          __threadfence();
+          st_release(my_prog, base + (unsigned)(s + 1));
+        }
+      }
+    }
+    // Completion (also after an aborted wait, so that no other warp blocks).
+    __syncwarp();
+    if (src < A.nsrc && lane == 0) {
+      __threadfence();
+      st_release(my_prog, base + (unsigned)T);
+    }
+  }
+}
+
 // Fill every node with Big and every branch record with "no sign".
 __global__ void fill3d_kernel(double* tt, uint8_t* rec, long long n) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
@@ -747,10 +1084,22 @@ __global__ void pencil_order_kernel(int PJ, int PK, int* order) {
 // ---------------------------------------------------------------- host side --
 
 // Launch shape of the sweep kernel: pencil width (2, 4, 8), steps between
-// progress publications (power of 2), coefficient source (1 arrays, 0 cells).
+// progress publications (power of 2), coefficient source (1 arrays, 0 cells),
+// and whether blocks of kTeamWarps sources step together with compacted
+// operators (the team kernel; single-model solves of 4+ sources).
 struct Tune3 {
-  int pencil, chunk, coef;
+  int pencil, chunk, coef, team;
 };
+
+static const void* team_kernel(int grad, bool coef, int pencil) {
+#define FTEIK_T(G, C, P) (const void*)sweep3d_team_kernel<G, C, P>
+#define FTEIK_TP(G, C) \
+  (pencil == 2 ? FTEIK_T(G, C, 2) : pencil == 8 ? FTEIK_T(G, C, 8) : FTEIK_T(G, C, 4))
+  if (grad != 0) return coef ? FTEIK_TP(true, true) : FTEIK_TP(true, false);
+  return coef ? FTEIK_TP(false, true) : FTEIK_TP(false, false);
+#undef FTEIK_TP
+#undef FTEIK_T
+}
 
 static const void* sweep_kernel(int grad, bool coef, int pencil, bool multi) {
 #define FTEIK_K(G, C, P, M) (const void*)sweep3d_kernel<G, C, P, M>
@@ -785,26 +1134,38 @@ static void tuned_store(const std::vector<long long>& key, const Tune3& t) {
 }
 
 // Default shape for `jobs` (model, source) pairs in flight, of which
-// `coef_sources` share one model's coefficients: with few jobs the solve is
-// bound by the latency of the pencil wavefront, and publishing progress
-// every step (chunk 1) lets downwind pencils start soonest; with many, the
-// FP64 pipe is the bound and fewer publications cost less.
-static Tune3 default_tune(int jobs, int coef_sources) {
-  const int chunk = jobs <= 2 ? 1 : jobs <= 8 ? 2 : kDefaultChunk;
-  return Tune3{kDefaultPencil, chunk, coef_sources >= kCoefMinSources ? 1 : 0};
+// `coef_sources` share one model's coefficients, with `items` (source,
+// pencil) work items per sweep (0: not a single-model solve).  Measured on
+// GB300 (sweep kernel, nsweep 2):
+//  * 1-2 sources are bound by the latency of the pencil wavefront;
+//    publishing progress every step (chunk 1) lets downwind pencils start
+//    soonest (17% faster than chunk 4 on 128x256x256);
+//  * up to ~100K items per sweep one warp per pencil wins (64 sources on
+//    96x128x128: 182 ms against 193 ms for the team kernel);
+//  * above that the team kernel wins (64 sources on 128x256x256: 989 against
+//    1067 ms), and from ~400K items it is best publishing every 16 steps
+//    (256 sources: 3734 ms against 3815 ms at chunk 4 and 4120 ms one warp
+//    per pencil).
+static Tune3 default_tune(int jobs, int coef_sources, long long items = 0) {
+  const int team = items >= 100000 ? 1 : 0;
+  const int chunk = jobs <= 2 ? 1 : jobs <= 8 ? 2 : (team && items >= 400000) ? 16 : kDefaultChunk;
+  return Tune3{kDefaultPencil, chunk, coef_sources >= kCoefMinSources ? 1 : 0, team};
 }
 
 // The shape a solve runs with: explicit options first, then a shape the
 // autotuner measured for this signature, then the defaults.
-static Tune3 resolve_tune(const std::vector<long long>& key, int jobs, int coef_sources) {
-  Tune3 t = default_tune(jobs, coef_sources);
+static Tune3 resolve_tune(const std::vector<long long>& key, int jobs, int coef_sources,
+                          long long items = 0) {
+  Tune3 t = default_tune(jobs, coef_sources, items);
   Tune3 m;
   if (tuned_lookup(key, &m)) t = m;
   const long long op = option_value(kOptSweepPencil), oc = option_value(kOptSweepChunk),
                   of = option_value(kOptSweepCoef);
+  const long long ot = option_value(kOptSweepTeam);
   if (op > 0) t.pencil = (int)op;
   if (oc > 0) t.chunk = (int)oc;
   if (of >= 0) t.coef = (int)of;
+  if (ot >= 0) t.team = (int)ot;
   return t;
 }
 
@@ -830,6 +1191,19 @@ static int launch_sweep(const void* kern, const Sweep3Args& A, long long items, 
 // "sweep_keep_test" = 0 turns it off.
 static int keep_test_enabled(double dz, double dx, double dy) {
   return dz == dx && dx == dy && option_value(kOptKeepTest) != 0 ? 1 : 0;
+}
+
+// Persistent launch of the team kernel: one block per item in flight.
+static int launch_team(const void* kern, const Sweep3Args& A, long long items, cudaStream_t st) {
+  int blocks = resident_blocks(kern, kTeamWarps * 32);
+  if (items < blocks) blocks = (int)items;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  timing_events(&ev0, &ev1);
+  if (ev0) FTEIK_CHECK(cudaEventRecord(ev0, st));
+  void* args[] = {(void*)&A};
+  FTEIK_CHECK(cudaLaunchKernel(kern, dim3(blocks), dim3(kTeamWarps * 32), args, 0, st));
+  if (ev1) FTEIK_CHECK(cudaEventRecord(ev1, st));
+  return kOk;
 }
 
 static void sweep_args_defaults(Sweep3Args& A) {
@@ -865,8 +1239,11 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
                     (0.0 <= y && y <= dy * ny);
     if (!ok) return kSourceOutOfBound;
   }
-  const Tune3 tune =
-      force ? *force : resolve_tune(single_key(nz, nx, ny, nsrc, grad), nsrc, nsrc);
+  const long long items_default =
+      (long long)nsrc * pencils_of(nx + 1, ny + 1, kDefaultPencil);
+  const Tune3 tune = force ? *force
+                           : resolve_tune(single_key(nz, nx, ny, nsrc, grad), nsrc, nsrc,
+                                          items_default);
   const int pw = tune.pencil, pk = 32 / pw;
   const int NZ = nz + 1, NX = nx + 1, NY = ny + 1;
   const int PJ = (NX + pw - 1) / pw, PK = (NY + pk - 1) / pk;
@@ -942,8 +1319,15 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
     A.spin_limit = spin_limit > 0 ? spin_limit : (1LL << 25);
     A.keep_test = keep_test_enabled(dz, dx, dy);
     A.o = o;
-    const long long items = (long long)nepochs * PJ * PK * nsrc;
-    const int rc = launch_sweep(sweep_kernel(grad, use_coef, pw, false), A, items, st);
+    int rc;
+    if (tune.team) {
+      A.ngroups = (nsrc + kTeamWarps - 1) / kTeamWarps;
+      rc = launch_team(team_kernel(grad, use_coef, pw), A,
+                       (long long)nepochs * PJ * PK * A.ngroups, st);
+    } else {
+      rc = launch_sweep(sweep_kernel(grad, use_coef, pw, false), A,
+                        (long long)nepochs * PJ * PK * nsrc, st);
+    }
     if (rc != kOk) return rc;
   }
   if (grad == 1) {
@@ -1243,8 +1627,10 @@ namespace {
 // coefficient source, each timed (sweep kernel only, CUDA events on the
 // stream) with one sweep per direction, the best of `reps` runs.
 template <class Run>
-int tune_search(Run run, int jobs, int coef_sources, int reps, Tune3* best, float* best_ms) {
-  Tune3 cur = default_tune(jobs, coef_sources);
+int tune_search(Run run, int jobs, int coef_sources, long long items, int reps, bool allow_team,
+                Tune3* best, float* best_ms) {
+  Tune3 cur = default_tune(jobs, coef_sources, items);
+  if (!allow_team) cur.team = 0;
   float cur_ms = 0.f;
   auto time_of = [&](const Tune3& t, float* ms) -> int {
     float b = 3.4e38f;
@@ -1263,15 +1649,19 @@ int tune_search(Run run, int jobs, int coef_sources, int reps, Tune3* best, floa
   if (rc != kOk) return rc;
   const int chunks[] = {1, 2, 4, 8, 16, 32};
   const int pencils[] = {2, 4, 8};
-  for (int pass = 0; pass < 3; ++pass) {
+  for (int pass = 0; pass < 4; ++pass) {
     Tune3 base = cur;
-    const int n = pass == 0 ? 6 : pass == 1 ? 3 : 2;
+    const int n = pass == 0 ? 2 : pass == 1 ? 6 : pass == 2 ? 3 : 2;
+    if (pass == 0 && !allow_team) continue;
     for (int q = 0; q < n; ++q) {
       Tune3 t = base;
-      if (pass == 0) t.chunk = chunks[q];
-      if (pass == 1) t.pencil = pencils[q];
-      if (pass == 2) t.coef = q;
-      if (t.chunk == cur.chunk && t.pencil == cur.pencil && t.coef == cur.coef) continue;
+      if (pass == 0) t.team = q;
+      if (pass == 1) t.chunk = chunks[q];
+      if (pass == 2) t.pencil = pencils[q];
+      if (pass == 3) t.coef = q;
+      if (t.chunk == cur.chunk && t.pencil == cur.pencil && t.coef == cur.coef &&
+          t.team == cur.team)
+        continue;
       float ms = 0.f;
       rc = time_of(t, &ms);
       if (rc != kOk) return rc;
@@ -1318,7 +1708,9 @@ extern "C" int fteik3d_autotune(const double* slow, int nz, int nx, int ny, doub
   Tune3 best;
   float ms = 0.f;
   const bool timing_was_on = kernel_timing_on();
-  const int rc = tune_search(run, nsrc, nsrc, 2, &best, &ms);
+  const int rc = tune_search(run, nsrc, nsrc,
+                             (long long)nsrc * pencils_of(nx + 1, ny + 1, kDefaultPencil), 2,
+                             true, &best, &ms);
   fteik_kernel_timing(timing_was_on ? 1 : 0);
   if (rc != kOk) return rc;
   tuned_store(single_key(nz, nx, ny, nsrc, grad), best);
@@ -1326,6 +1718,7 @@ extern "C" int fteik3d_autotune(const double* slow, int nz, int nx, int ny, doub
     shape[0] = best.pencil;
     shape[1] = best.chunk;
     shape[2] = best.coef;
+    shape[3] = best.team;
   }
   if (best_ms) *best_ms = ms;
   return kOk;
@@ -1352,7 +1745,7 @@ extern "C" int fteik3d_batch_autotune(int nmodel, const double* const* slow, con
   Tune3 best;
   float ms = 0.f;
   const bool timing_was_on = kernel_timing_on();
-  const int rc = tune_search(run, (int)total, (int)(total / nmodel), 1, &best, &ms);
+  const int rc = tune_search(run, (int)total, (int)(total / nmodel), 0, 1, false, &best, &ms);
   fteik_kernel_timing(timing_was_on ? 1 : 0);
   if (rc != kOk) return rc;
   tuned_store(batch_key(nmodel, dims, nsrc, grad), best);
@@ -1360,6 +1753,7 @@ extern "C" int fteik3d_batch_autotune(int nmodel, const double* const* slow, con
     shape[0] = best.pencil;
     shape[1] = best.chunk;
     shape[2] = best.coef;
+    shape[3] = 0;
   }
   if (best_ms) *best_ms = ms;
   return kOk;

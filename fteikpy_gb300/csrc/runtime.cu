@@ -61,7 +61,7 @@ int grid_for(long long n, int threads) {
   return (int)blocks;
 }
 
-static long long g_options[kOptCount] = {-1, -1, -1, -1};
+static long long g_options[kOptCount] = {-1, -1, -1, -1, -1};
 
 long long option_value(int opt) { return (opt >= 0 && opt < kOptCount) ? g_options[opt] : -1; }
 
@@ -112,6 +112,10 @@ extern "C" int fteik_set_option(const char* name, long long value) {
     g_options[kOptKeepTest] = value < 0 ? -1 : (value ? 1 : 0);
     return kOk;
   }
+  if (std::strcmp(name, "sweep_team") == 0) {
+    g_options[kOptSweepTeam] = value < 0 ? -1 : (value ? 1 : 0);
+    return kOk;
+  }
   return kInvalidArgument;
 }
 
@@ -121,6 +125,7 @@ extern "C" int fteik_get_option(const char* name, long long* value) {
   else if (std::strcmp(name, "sweep_pencil") == 0) *value = g_options[kOptSweepPencil];
   else if (std::strcmp(name, "sweep_chunk") == 0) *value = g_options[kOptSweepChunk];
   else if (std::strcmp(name, "sweep_keep_test") == 0) *value = g_options[kOptKeepTest];
+  else if (std::strcmp(name, "sweep_team") == 0) *value = g_options[kOptSweepTeam];
   else return kInvalidArgument;
   return kOk;
 }

@@ -34,7 +34,8 @@ enum Option : int {
   kOptSweepPencil = 1,  // 3D pencil width along x: 2, 4 or 8 (the pencil is w x 32/w)
   kOptSweepChunk = 2,   // 3D steps between progress publications: 1, 2, 4, ... 64
   kOptKeepTest = 3,     // 3D unchanged-node test before the 2D/3D operators: 0 off
-  kOptCount = 4,
+  kOptSweepTeam = 4,    // 3D team kernel (compacted operators): 1 on, 0 off
+  kOptCount = 5,
 };
 long long option_value(int opt);
 

@@ -46,7 +46,9 @@ int fteik_kernel_timing(int on);
  * 8 cells around each node, 1 makes it read precomputed coefficient arrays
  * (faster for batches of sources, which reuse them). "sweep_pencil": pencil
  * width along x, 2, 4 or 8. "sweep_chunk": steps between progress
- * publications, a power of 2 up to 64. "sweep_keep_test": 0 turns off the
+ * publications, a power of 2 up to 64. "sweep_team": 1 runs single-model
+ * solves with the team kernel (compacted operators; the default from 4
+ * sources), 0 with one warp per pencil. "sweep_keep_test": 0 turns off the
  * test that skips the 2D/3D operators of nodes that provably keep their value
  * (grids with equal spacings only). Results are identical for every setting.
  * fteik_get_option reads a knob back. */
@@ -125,13 +127,17 @@ int fteik3d_solve_batch(int nmodel, const double* const* slow, const int* dims,
  * Launch shape of the 3D sweep kernel: pencil width along x (2, 4 or 8; a
  * pencil is w x 32/w node columns, one per lane of a warp), steps between
  * progress publications (a power of 2, the hyperplane chunk), and the
- * coefficient source (1 precomputed arrays, 0 slowness cells). The autotuner
+ * coefficient source (1 precomputed arrays, 0 slowness cells), and team mode
+ * (1: blocks of 4 sources step through a pencil together and evaluate the
+ * 2D/3D operators their lanes need packed 32 to a warp instruction; single
+ * model only). The autotuner
  * times candidate shapes on the caller's problem (one sweep per direction,
  * sweep kernel only), keeps the fastest for that problem signature (cell
  * counts, source counts, gradients) for the rest of the process, and returns
- * it in shape[3] = {pencil, chunk, coef} and its time in best_ms. Solves of
- * the same signature then use it unless fteik_set_option overrides a part
- * ("sweep_pencil", "sweep_chunk", "sweep_coef"; -1 = automatic). The
+ * it in shape[4] = {pencil, chunk, coef, team} and its time in best_ms.
+ * Solves of the same signature then use it unless fteik_set_option overrides
+ * a part ("sweep_pencil", "sweep_chunk", "sweep_coef", "sweep_team";
+ * -1 = automatic). The
  * arguments are those of fteik3d_solve / fteik3d_solve_batch (the outputs are
  * overwritten). No counterpart in the reference. */
 int fteik3d_autotune(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,

@@ -34,7 +34,8 @@ def sources_in(rng, shape, d, n):
 def options():
     lib = _lib.load()
     yield lib
-    for name in (b"sweep_pencil", b"sweep_chunk", b"sweep_coef", b"sweep_keep_test"):
+    for name in (b"sweep_pencil", b"sweep_chunk", b"sweep_coef", b"sweep_keep_test",
+                 b"sweep_team"):
         lib.fteik_set_option(name, -1)
     lib.fteik_clear_tuning()
 
@@ -42,15 +43,18 @@ def options():
 @pytest.mark.parametrize("pencil", [2, 4, 8])
 @pytest.mark.parametrize("chunk", [1, 4, 32])
 @pytest.mark.parametrize("coef", [0, 1])
-def test_every_launch_shape_gives_the_reference_bits(options, pencil, chunk, coef):
+@pytest.mark.parametrize("team", [0, 1])
+def test_every_launch_shape_gives_the_reference_bits(options, pencil, chunk, coef, team):
     lib = options
     assert lib.fteik_set_option(b"sweep_pencil", pencil) == 0
     assert lib.fteik_set_option(b"sweep_chunk", chunk) == 0
     assert lib.fteik_set_option(b"sweep_coef", coef) == 0
+    assert lib.fteik_set_option(b"sweep_team", team) == 0
     rng = np.random.default_rng(pencil * 100 + chunk * 10 + coef)
     shape, d = (17, 23, 37), (9.0, 11.0, 10.0)
     v = gradient_model(shape, d, 3)
-    src = sources_in(rng, shape, d, 3)
+    # 3 and 6 sources: the team kernel's last group of 4 has idle warps
+    src = sources_in(rng, shape, d, 3 + 3 * team)
     tt_o, tg_o, _ = O.solve3d(1.0 / v, d, src, 2, True)
     tts = fp.Eikonal3D(v, d).solve(src, nsweep=2, return_gradient=True)
     assert bitwise(np.stack([t.grid for t in tts]), tt_o)
@@ -128,7 +132,7 @@ def test_autotune_single_and_batch(options):
     ref = np.stack([t.grid for t in eik.solve(src, nsweep=2)])
     best = fp.autotune(eik, src)
     assert best["pencil"] in (2, 4, 8) and best["chunk"] in (1, 2, 4, 8, 16, 32)
-    assert best["coef"] in (0, 1) and best["ms"] > 0
+    assert best["coef"] in (0, 1) and best["team"] in (0, 1) and best["ms"] > 0
     assert bitwise(np.stack([t.grid for t in eik.solve(src, nsweep=2)]), ref)
     solvers, sources, cases = uneven_batch(9, 5)
     best = fp.autotune(solvers, sources)
@@ -152,6 +156,7 @@ def test_unchanged_node_test_gives_the_same_bits(options, grad):
     res = {}
     for on in (1, 0):
         assert lib.fteik_set_option(b"sweep_keep_test", on) == 0
+        assert lib.fteik_set_option(b"sweep_team", 1) == 0
         tts = fp.Eikonal3D(v, d).solve(src, nsweep=3, return_gradient=grad)
         res[on] = (np.stack([t.grid for t in tts]),
                    np.stack([t._gradient.cpu().numpy() for t in tts]) if grad else None)
@@ -159,3 +164,26 @@ def test_unchanged_node_test_gives_the_same_bits(options, grad):
     if grad:
         assert bitwise(res[0][1], res[1][1])
     assert bitwise(res[1][0], O.solve3d(1.0 / v, d, src, 3, False)[0])
+
+
+@pytest.mark.parametrize("nsrc", [4, 9, 16])
+def test_team_kernel_equals_warp_kernel_on_a_layered_model(options, nsrc):
+    """Team and warp-per-pencil kernels on an equal-spacing layered model
+    (the unchanged-node test active), with gradients: same bits, and the
+    oracle's."""
+    lib = options
+    rng = np.random.default_rng(nsrc)
+    shape, d = (33, 40, 29), (10.0, 10.0, 10.0)
+    v = gradient_model(shape, d, nsrc)
+    v[15:] *= 1.6
+    src = sources_in(rng, shape, d, nsrc)
+    src[: nsrc // 2, 0] = 0.0
+    out = {}
+    for team in (0, 1):
+        lib.fteik_set_option(b"sweep_team", team)
+        tts = fp.Eikonal3D(v, d).solve(src, nsweep=2, return_gradient=True)
+        out[team] = (np.stack([t.grid for t in tts]),
+                     np.stack([t._gradient.cpu().numpy() for t in tts]))
+    assert bitwise(out[0][0], out[1][0]) and bitwise(out[0][1], out[1][1])
+    tt_o, tg_o, _ = O.solve3d(1.0 / v, d, src, 2, True)
+    assert bitwise(out[1][0], tt_o) and bitwise(out[1][1], tg_o)

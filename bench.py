@@ -43,10 +43,10 @@ NREC = 400
 NSWEEP = 2
 FLOP_PER_UPDATE = 160  # algorithmic FP64 operations of one 3D node update
 BYTES_PER_UPDATE = 25  # slowness + tt read + tt write (8 B each) + 1 B branch record
-# DRAM bytes (read + write) per node update of the sweep kernel, measured by
-# ncu on the 32-source 64x128x128 case (profiles/sweep3d_small_full.md:
-# 7.354 GB + 0.872 GB for 537 M updates); the full launch is scaled from it.
-TRAFFIC_BYTES_PER_UPDATE = (7.354e9 + 0.872e9) / 536870912
+# DRAM bytes (read + write) per node update of the team sweep kernel, measured
+# by ncu on the 192-source 64x128x128 case (profiles/sweep3d_team_small_full.md:
+# 87.147 GB + 9.593 GB for 3.221 G updates); the full launch is scaled from it.
+TRAFFIC_BYTES_PER_UPDATE = (87.147e9 + 9.593e9) / 3221225472
 
 
 def smooth2d(rng, shape, sigma):
@@ -657,11 +657,12 @@ def main():
     ap.add_argument("--dump", default=None,
                     help="--config 5: save the gradient and the finite differences (.npz)")
     ap.add_argument("--small", action="store_true",
-                    help="profiling case: 32 sources on a 64x128x128 grid (277 MB of traveltimes, > L2)")
+                    help="profiling case: 192 sources on a 64x128x128 grid (1.7 GB of traveltimes, "
+                         "> L2; 108K items per sweep, so the same team kernel as the full step)")
     args = ap.parse_args()
     if args.small:
         global SHAPE, NSRC
-        SHAPE, NSRC = (64, 128, 128), 32
+        SHAPE, NSRC = (64, 128, 128), 192
     if args.impl == "reference":
         return run_reference(args)
     if args.config in (1, 2, 4, 5):
@@ -734,6 +735,7 @@ def main():
     sweep = float(np.mean(sweep_ms))
 
     # roofline of the sweep kernel (one launch = all sweeps of all sources)
+    kernel_name = lib.fteik_last_sweep_kernel().decode()
     updates = updates_per_source() * NSRC
     scratch = torch.empty(152 * 8 * 256, dtype=torch.float64, device=dev)
     peak = __import__("ctypes").c_double()
@@ -816,7 +818,7 @@ def main():
             },
             "roofline": {
                 "bound": "fp64",
-                "kernel": "sweep3d_kernel",
+                "kernel": kernel_name,
                 "achieved": achieved_tf,
                 "peak": peak_tf,
                 "unit": "TFLOP/s",
@@ -825,13 +827,14 @@ def main():
                 "peak_source": "DFMA loop measured in this run (fteik_fp64_peak)",
                 "note": "algorithmic work counts every node update of the reference's loops; "
                         "the kernel skips the 2D/3D operators of nodes that provably keep "
-                        "their value (exact, bitwise-tested), so frac can pass 1; ncu shows "
-                        "the FP64 pipe 72% busy on the 32-source case",
+                        "their value (exact, bitwise-tested), so frac can pass 1; ncu on the "
+                        "192-source case: FP64 pipe 77% busy, useful FP64 lane work 66% of "
+                        "peak",
                 "kernel_ms": sweep,
                 "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
                         "frac": hbm_gbs / hbm_peak, "bytes_per_update": BYTES_PER_UPDATE},
                 "traffic": traffic,
-                "traffic_source": "ncu DRAM bytes per update on the 32-source 64x128x128 "
+                "traffic_source": "ncu DRAM bytes per update on the 192-source 64x128x128 "
                                   "case, scaled by updates per launch",
             },
             "e2e": {

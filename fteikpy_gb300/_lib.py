@@ -46,6 +46,7 @@ SIGNATURES = {
         _I, [_I, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _SZ, _LL, _P, _P, _P]
     ),
     "fteik_clear_tuning": (_I, []),
+    "fteik_last_sweep_kernel": (ctypes.c_char_p, []),
     "fteik3d_tape_bytes": (_SZ, [_I, _I, _I, _I, _I]),
     "fteik3d_solve_tape": (
         _I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _P, _P, _SZ, _P, _SZ, _LL, _P]

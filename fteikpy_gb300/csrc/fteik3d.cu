@@ -1193,6 +1193,9 @@ static int keep_test_enabled(double dz, double dx, double dy) {
   return dz == dx && dx == dy && option_value(kOptKeepTest) != 0 ? 1 : 0;
 }
 
+// Name of the sweep kernel the last 3D solve launched (measurement reports).
+static const char* g_last_sweep_kernel = "none";
+
 // Persistent launch of the team kernel: one block per item in flight.
 static int launch_team(const void* kern, const Sweep3Args& A, long long items, cudaStream_t st) {
   int blocks = resident_blocks(kern, kTeamWarps * 32);
@@ -1322,9 +1325,11 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
     int rc;
     if (tune.team) {
       A.ngroups = (nsrc + kTeamWarps - 1) / kTeamWarps;
+      g_last_sweep_kernel = "sweep3d_team_kernel";
       rc = launch_team(team_kernel(grad, use_coef, pw), A,
                        (long long)nepochs * PJ * PK * A.ngroups, st);
     } else {
+      g_last_sweep_kernel = "sweep3d_kernel";
       rc = launch_sweep(sweep_kernel(grad, use_coef, pw, false), A,
                         (long long)nepochs * PJ * PK * nsrc, st);
     }
@@ -1598,6 +1603,7 @@ static int solve_batch_impl(int nmodel, const double* const* slow, const int* di
     A.nepochs = (int)nepochs;
     A.chunk = tune.chunk;
     A.spin_limit = spin_limit > 0 ? spin_limit : (1LL << 25);
+    g_last_sweep_kernel = "sweep3d_kernel (models)";
     const int rc = launch_sweep(sweep_kernel(grad, use_coef, pw, true), A,
                                 (long long)nepochs * (long long)items.size(), st);
     if (rc != kOk) return rc;
@@ -1758,6 +1764,8 @@ extern "C" int fteik3d_batch_autotune(int nmodel, const double* const* slow, con
   if (best_ms) *best_ms = ms;
   return kOk;
 }
+
+extern "C" const char* fteik_last_sweep_kernel(void) { return g_last_sweep_kernel; }
 
 extern "C" int fteik_clear_tuning(void) {
   std::lock_guard<std::mutex> lock(g_tune_mu);

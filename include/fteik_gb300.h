@@ -151,6 +151,9 @@ int fteik3d_batch_autotune(int nmodel, const double* const* slow, const int* dim
                            int* shape, float* best_ms, void* stream);
 /* Forget every measured shape. */
 int fteik_clear_tuning(void);
+/* Name of the sweep kernel the last 3D solve on this host thread launched
+ * ("sweep3d_team_kernel", "sweep3d_kernel", "sweep3d_kernel (models)"). */
+const char* fteik_last_sweep_kernel(void);
 
 /* 3D solve that allocates nothing. No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc or hand over a device workspace (a

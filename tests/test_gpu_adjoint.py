@@ -127,3 +127,24 @@ def test_reverse_pass_wait_timeout_is_reported_and_recoverable(monkeypatch):
     _, g = gpu_gradient(v0, src, rec, nsweep, t_obs)
     go = oracle_velocity_gradient(v0, src, rec, nsweep, t_obs)
     assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()
+
+
+@pytest.mark.parametrize("team", [0, 1])
+def test_adjoint_through_either_sweep_kernel(team):
+    """The taped forward runs in either sweep kernel (large batches use the
+    team kernel): the gradient is the oracle adjoint's in both."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    lib.fteik_set_option(b"sweep_team", team)
+    try:
+        shape, nsweep = (11, 13, 15), 2
+        src, rec = geometry(shape, 6, 20, 8)
+        t_obs = oracle_times(velocity(shape, True), src, rec, nsweep)
+        v0 = velocity(shape, False)
+        T, g = gpu_gradient(v0, src, rec, nsweep, t_obs)
+        assert np.array_equal(T, oracle_times(v0, src, rec, nsweep))
+        go = oracle_velocity_gradient(v0, src, rec, nsweep, t_obs)
+        assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()
+    finally:
+        lib.fteik_set_option(b"sweep_team", -1)

@@ -97,13 +97,48 @@ __device__ __forceinline__ void grad_at(const Axes& ax, const double* g, const d
   }
 }
 
-// _ray3d / _ray2d, _ray3d.py:9-120 and _ray2d.py:9-91.
+// Component `comp` of grad_at (the same lookup, weights and blend).
 template <int ND>
+__device__ __forceinline__ double grad_comp(const Axes& ax, const double* g, const double* p,
+                                            int comp) {
+  if (ND == 3) {
+    if (!inside3(ax.a[0], ax.n[0], ax.a[1], ax.n[1], ax.a[2], ax.n[2], p[0], p[1], p[2]))
+      return CUDART_NAN;
+    const Cell3 c = locate3(ax.a[0], ax.n[0], ax.a[1], ax.n[1], ax.a[2], ax.n[2], p[0], p[1], p[2]);
+    double w[8], q[8];
+    weights3(c, p[0], p[1], p[2], w);
+    corners3(g + comp, 3, c, ax.n[1], ax.n[2], q);
+    return blend3(c, q, w);
+  } else {
+    if (!inside2(ax.a[0], ax.n[0], ax.a[1], ax.n[1], p[0], p[1])) return CUDART_NAN;
+    const Cell2 c = locate2(ax.a[0], ax.n[0], ax.a[1], ax.n[1], p[0], p[1]);
+    double w[4], q[4];
+    weights2(c, p[0], p[1], w);
+    corners2(g + comp, 2, c, ax.n[1], q);
+    double vq = q[0] * w[0];
+    vq += q[1] * w[1];
+    vq += q[2] * w[2];
+    vq += q[3] * w[3];
+    vq /= fabs((c.x2 - c.x1) * (c.y2 - c.y1));
+    return vq;
+  }
+}
+
+// _ray3d / _ray2d, _ray3d.py:9-120 and _ray2d.py:9-91.
+// L lanes trace one ray: with L = 4, lanes 0..ND-1 of the group each blend
+// one gradient component and the group shares them, so a few rays (one
+// source's receivers) take fewer dependent FP64 instructions per step; the
+// other work is done identically by every lane and lane 0 writes.
+template <int ND, int L>
 __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, const int* gidx,
                            const double* ends, int nrays, const double* sources,
                            double stepsize, int max_step, int honor_grid, double* rays,
                            int* counts, int* status) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int r = (int)(tid / L);
+  const int sub = (int)(tid % L);
+  const bool writer = sub == 0;
+  const unsigned gmask = L == 1 ? 0u : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
   if (r >= nrays) return;
   const int gi = gidx ? gidx[r] : 0;
   const double* g = ttgrad + (long long)gi * gstride;
@@ -114,11 +149,11 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
     src[q] = sources[ND * gi + q];
     pcur[q] = ends[ND * r + q];
   }
-  counts[r] = 0;
+  if (writer) counts[r] = 0;
 #pragma unroll
   for (int q = 0; q < ND; ++q) {
     if (!(__ldg(ax.a[q]) <= pcur[q] && pcur[q] <= __ldg(ax.a[q] + ax.n[q] - 1))) {
-      status[r] = kEndPointOutOfBound;
+      if (writer) status[r] = kEndPointOutOfBound;
       return;
     }
   }
@@ -135,8 +170,10 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
   }
   double* ray = rays + (long long)r * max_step * ND;
   int count = 1;
+  if (writer) {
 #pragma unroll
-  for (int q = 0; q < ND; ++q) ray[q] = pcur[q];
+    for (int q = 0; q < ND; ++q) ray[q] = pcur[q];
+  }
   // The reference loops until the ray reaches the source or max_step points
   // are recorded; with honor_grid a step inside a cell records nothing, so
   // the number of iterations is capped as well (a cap the reference does not
@@ -144,14 +181,20 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
   const long long max_iter = 64LL * max_step + 4096;
   for (long long iter = 0;; ++iter) {
     if (iter >= max_iter) {
-      status[r] = kMaxStepReached;
+      if (writer) status[r] = kMaxStepReached;
       return;
     }
     const double dd = ND == 3 ? dist3(src[0], src[1], src[2], pcur[0], pcur[1], pcur[2])
                               : dist2(src[0], src[1], pcur[0], pcur[1]);
     if (!(dd >= stepsize)) break;
     double gv[ND];
-    grad_at<ND>(ax, g, pcur, gv);
+    if (L == 1) {
+      grad_at<ND>(ax, g, pcur, gv);
+    } else {
+      const double mine = sub < ND ? grad_comp<ND>(ax, g, pcur, sub) : 0.0;
+#pragma unroll
+      for (int q = 0; q < ND; ++q) gv[q] = __shfl_sync(gmask, mine, q, L);
+    }
     double gsq = gv[0] * gv[0] + gv[1] * gv[1];
     if (ND == 3) gsq = gsq + gv[ND - 1] * gv[ND - 1];
     const double gn = sqrt(gsq);
@@ -190,8 +233,10 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
           upper[q] = __ldg(a + imin(i + 1, n - 1));
           hit = hit && (i == isrc[q]);
         }
+        if (writer) {
 #pragma unroll
-        for (int q = 0; q < ND; ++q) ray[count * ND + q] = pcur[q];
+          for (int q = 0; q < ND; ++q) ray[count * ND + q] = pcur[q];
+        }
         count += 1;
         if (hit) break;
       }
@@ -203,19 +248,21 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
         v = lo > v ? lo : v;
         v = hi < v ? hi : v;
         pcur[q] = v;
-        ray[count * ND + q] = v;
+        if (writer) ray[count * ND + q] = v;
       }
       count += 1;
     }
     if (count >= max_step) {
-      status[r] = kMaxStepReached;
+      if (writer) status[r] = kMaxStepReached;
       return;
     }
   }
+  if (writer) {
 #pragma unroll
-  for (int q = 0; q < ND; ++q) ray[count * ND + q] = src[q];
-  counts[r] = count;
-  status[r] = kOk;
+    for (int q = 0; q < ND; ++q) ray[count * ND + q] = src[q];
+    counts[r] = count;
+    status[r] = kOk;
+  }
 }
 
 // Reverse each ray (source first, as ray3d returns ray[count::-1]) and pack
@@ -251,9 +298,19 @@ static int launch_rays(const double* const* axes, const int* n, const double* tt
     if (q < ND && n[q] < 2) return kInvalidArgument;
   }
   if (nrays == 0) return kOk;
-  ray_kernel<ND><<<(nrays + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
-      ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, max_step, honor_grid,
-      rays, counts, status);
+  // Four lanes per ray while every ray's group fits on the GPU at once (one
+  // source's receivers); one lane per ray for large batches, which are bound
+  // by throughput rather than by the latency of a step.
+  if ((long long)nrays * 4 <= 64LL * 1024) {
+    const long long threads = (long long)nrays * 4;
+    ray_kernel<ND, 4><<<(unsigned)((threads + 63) / 64), 64, 0, (cudaStream_t)stream>>>(
+        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, max_step,
+        honor_grid, rays, counts, status);
+  } else {
+    ray_kernel<ND, 1><<<(nrays + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
+        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, max_step,
+        honor_grid, rays, counts, status);
+  }
   FTEIK_CHECK(cudaGetLastError());
   return kOk;
 }

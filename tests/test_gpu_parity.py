@@ -336,3 +336,29 @@ def test_solve3d_both_coefficient_sources(coef):
         assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)
     finally:
         lib.fteik_set_option(b"sweep_coef", -1)
+
+
+def test_rays_with_one_and_four_lanes_per_ray_agree():
+    """Large ray batches run one lane per ray, small ones four (one gradient
+    component per lane): the same rays bit for bit, and the oracle's."""
+    from fteikpy_gb300._grid import trace_rays
+
+    rng = np.random.default_rng(31)
+    shape, d = (20, 30, 25), (10.0, 10.0, 10.0)
+    v = layered3d(shape, 31)
+    src = np.array([0.0, 140.0, 120.0])
+    tt = fp.Eikonal3D(v, d).solve(src, nsweep=2, return_gradient=True)
+    ax = [_device.to_device(a) for a in O.axes(tt.shape, d, np.zeros(3))]
+    ext = np.array(shape) * np.array(d)
+    ends = rng.uniform(0.0, 1.0, (16400, 3)) * ext
+    g = tt._gradient.contiguous()
+    max_dist = 2.0 * sum((n * h) ** 2 for n, h in zip(tt.shape, d)) ** 0.5
+    max_step = int(max_dist / 10.0)
+    many = trace_rays(3, ax, g, None, ends, src[None], 10.0, max_step, False)
+    few = trace_rays(3, ax, g, None, ends[:400], src[None], 10.0, max_step, False)
+    assert all(np.array_equal(a, b) for a, b in zip(many[:400], few))
+    tg_o = O.solve3d(1.0 / v, d, [src], 2, True)[1][0]
+    sample = rng.choice(len(ends), 40, replace=False)
+    ref = O.raytrace(O.axes(tt.shape, d, np.zeros(3)), tg_o, ends[sample], src, 10.0, max_step,
+                     False)
+    assert all(np.array_equal(many[i], r) for i, r in zip(sample, ref))

@@ -95,13 +95,29 @@ def trace_rays_device(nd, axes, ttgrad, grid_index, ends, sources, stepsize, max
     (fteikpy/_fteik/_ray3d.py:33-34,115-116).
     """
     lib = _lib.load()
+    dev = _device.device()
+    rays, counts, status, n = _launch_rays(
+        lib, nd, axes, ttgrad, grid_index, ends, sources, stepsize, max_step, honor_grid,
+        grad_stride,
+    )
+    if n == 0:
+        return (torch.empty((0, nd), dtype=torch.float64, device=dev),
+                torch.zeros(0, dtype=torch.int64, device=dev))
+    lengths = counts.to(torch.int64) + 1
+    packed, _ = _pack_rays(lib, nd, rays, n, max_step, counts, status, lengths)
+    return packed, lengths
+
+
+def _launch_rays(lib, nd, axes, ttgrad, grid_index, ends, sources, stepsize, max_step,
+                 honor_grid, grad_stride):
+    """Launch the ray kernel; return (rays, counts, status, nrays) on the device."""
     if max_step < 2:
         raise ValueError("max_step must be at least 2")
     dev = _device.device()
     e = ends if isinstance(ends, torch.Tensor) else _device.to_device(np.ascontiguousarray(ends, dtype=np.float64))
     n = e.shape[0]
     if n == 0:
-        return torch.empty((0, nd), dtype=torch.float64, device=dev), torch.zeros(0, dtype=torch.int64, device=dev)
+        return None, None, None, 0
     src = sources if isinstance(sources, torch.Tensor) else _device.to_device(np.ascontiguousarray(sources, dtype=np.float64))
     rays = torch.empty((n, max_step, nd), dtype=torch.float64, device=dev)
     counts = torch.empty(n, dtype=torch.int32, device=dev)
@@ -122,36 +138,46 @@ def trace_rays_device(nd, axes, ttgrad, grid_index, ends, sources, stepsize, max
             _device.ptr(status), _device.stream(),
         )
     _lib.check(rc, "raytrace")
-    worst = int(status.max().item())
+    return rays, counts, status, n
+
+
+def _pack_rays(lib, nd, rays, n, max_step, counts, status, lengths):
+    """Check the per-ray status and pack the rays source first; one host
+    round trip brings back the worst status, the total length and the
+    per-ray lengths. Returns (packed device rays, host lengths)."""
+    dev = rays.device
+    offsets = torch.cumsum(lengths, 0) - lengths
+    info = torch.cat([status.max().to(torch.int64).reshape(1), lengths]).cpu().numpy()
+    worst, host_lengths = int(info[0]), info[1:]
     if worst != _lib.OK:
         st = status.cpu().numpy()
         if (st == _lib.END_POINT_OUT_OF_BOUND).any():
             raise ValueError("end point out of bound")
         raise RuntimeError("maximum number of steps reached")
-    lengths = counts.to(torch.int64) + 1
-    offsets = torch.cumsum(lengths, 0) - lengths
-    total = int(lengths.sum().item())
-    packed = torch.empty((total, nd), dtype=torch.float64, device=dev)
+    packed = torch.empty((int(host_lengths.sum()), nd), dtype=torch.float64, device=dev)
     rc = lib.fteik_ray_pack(
         nd, _device.ptr(rays), n, max_step, _device.ptr(counts), _device.ptr(offsets),
         _device.ptr(packed), _device.stream(),
     )
     _lib.check(rc, "raytrace")
-    return packed, lengths
+    return packed, host_lengths
 
 
 def trace_rays(nd, axes, ttgrad, grid_index, ends, sources, stepsize, max_step, honor_grid,
                grad_stride=0):
     """``trace_rays_device`` followed by the copy to the host: a list of NumPy
     rays, as ``ray3d`` / ``ray2d`` return for several end points."""
-    packed, lengths = trace_rays_device(
-        nd, axes, ttgrad, grid_index, ends, sources, stepsize, max_step, honor_grid, grad_stride
+    lib = _lib.load()
+    rays, counts, status, n = _launch_rays(
+        lib, nd, axes, ttgrad, grid_index, ends, sources, stepsize, max_step, honor_grid,
+        grad_stride,
     )
-    if lengths.numel() == 0:
+    if n == 0:
         return []
+    lengths = counts.to(torch.int64) + 1
+    packed, host_lengths = _pack_rays(lib, nd, rays, n, max_step, counts, status, lengths)
     flat = packed.cpu().numpy()
-    cuts = np.cumsum(lengths.cpu().numpy())[:-1]
-    return np.split(flat, cuts)
+    return np.split(flat, np.cumsum(host_lengths)[:-1])
 
 
 class TraveltimeGrid2D(BaseGrid2D, BaseTraveltime, _TraveltimeMixin):

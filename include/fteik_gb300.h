@@ -90,7 +90,12 @@ int fteik3d_solve(const double* slow, int nz, int nx, int ny, double dz, double 
                   double* ttgrad, double* vzero, void* workspace, size_t workspace_bytes,
                   long long spin_limit, void* stream);
 /* Same work, enqueued on `stream` without waiting; the status is read later
- * with fteik_workspace_status(). Host-side argument errors return at once. */
+ * with fteik_workspace_status(). Host-side argument errors return at once.
+ * Everything it enqueues can be captured in a CUDA graph when `sources` is
+ * pinned host memory: a replay copies the sources from that buffer again (so
+ * new positions can be written between replays; the bounds check runs at
+ * capture time only, so they must stay inside the model) and re-runs every
+ * kernel. With kernel timing on, the timing events are captured too. */
 int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, double dz, double dx,
                         double dy, const double* sources, int nsrc, int nsweep, int grad,
                         double* tt, double* ttgrad, double* vzero, void* workspace,

@@ -85,52 +85,74 @@ __device__ double delta2(double t1, double tauv, double taue, double tauev, doub
                  4.0 * ((double)sgntx * txc * dxi * ta + (double)sgntz * tzc * dzi * tb) +
                  4.0 * (vzero * vzero - vref * vref);
   double dpoly = bpoly * bpoly - 4.0 * apoly * cpoly;
-  return dpoly >= 0.0 ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
+  return fle(0.0, dpoly) ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
 }
 
-// One node update, _fteik2d.py:70-187.  NZ, NX are node counts.  Comparisons
-// are IEEE comparisons here (not integer keys): after a source on the model's
-// far boundary the reference's first propagation can leave NaN in tt, and
-// Python's comparison and min semantics on NaN must be kept.
-template <bool GRAD>
-__device__ __forceinline__ void node_update2d(double* tt, uint8_t* rec, const double* slow,
-                                              const Ops2& o, const Source2& sp, int i, int j,
-                                              int sgnvz, int sgnvx, int sgntz, int sgntx,
-                                              int NZ, int NX) {
+// The inputs of one node update that do not depend on the previous node of
+// the pass: the previous column's te and tev, the node's own old value t0, and
+// the five slowness cells of the operators.
+struct In2 {
+  double te, tev, t0, sz0, sz1, sx0, sx1, s2;
+};
+
+__device__ __forceinline__ In2 load_in2(const double* tt, const double* slow, int i, int j,
+                                        int sgnvz, int sgnvx, int sgntz, int sgntx, int NZ,
+                                        int NX) {
   const int nxc = NX - 1;
   const int i1 = i - sgnvz, j1 = j - sgnvx;
   const long long n = (long long)i * NX + j;
-  const double tv = tt[n - (long long)sgntz * NX];
-  const double te = tt[n - sgntx];
-  const double tev = tt[n - (long long)sgntz * NX - sgntx];
+  In2 q;
+  q.te = tt[n - sgntx];
+  q.tev = tt[n - (long long)sgntz * NX - sgntx];
+  q.t0 = tt[n];
+  q.sz0 = __ldg(slow + (long long)i1 * nxc + imax(j - 1, 0));
+  q.sz1 = __ldg(slow + (long long)i1 * nxc + imin(j, NX - 2));
+  q.sx0 = __ldg(slow + (long long)imax(i - 1, 0) * nxc + j1);
+  q.sx1 = __ldg(slow + (long long)imin(i, NZ - 2) * nxc + j1);
+  q.s2 = __ldg(slow + (long long)i1 * nxc + j1);
+  return q;
+}
 
-  double vref = pmin(slow[(long long)i1 * nxc + imax(j - 1, 0)], slow[(long long)i1 * nxc + imin(j, NX - 2)]);
+// One node update, _fteik2d.py:70-187, from tv (the previous node of the
+// pass) and the other inputs.  Comparisons are IEEE comparisons here (not
+// integer keys): after a source on the model's far boundary the reference's
+// first propagation can leave NaN in tt, and Python's comparison and min
+// semantics on NaN must be kept.  Returns the node's value after the update.
+template <bool GRAD>
+__device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const Ops2& o,
+                                                const Source2& sp, int i, int j, int sgntz,
+                                                int sgntx, int NX, double tv, const In2& q) {
+  const long long n = (long long)i * NX + j;
+  const double te = q.te, tev = q.tev;
+  double vref = pmin(q.sz0, q.sz1);
   const double t1d1 = tv + o.dz * vref;
-  vref = pmin(slow[(long long)imax(i - 1, 0) * nxc + j1], slow[(long long)imin(i, NZ - 2) * nxc + j1]);
+  vref = pmin(q.sx0, q.sx1);
   const double t1d2 = te + o.dx * vref;
-  const double t1d = t1d2 < t1d1 ? t1d2 : t1d1;
+  const double t1d = flt(t1d2, t1d1) ? t1d2 : t1d1;
 
   double t2d = kBig;
-  vref = slow[(long long)i1 * nxc + j1];
+  vref = q.s2;
   const int di = i - sp.zsi, dj = j - sp.xsi;
   if (di > kEpsin || di < -kEpsin || dj > kEpsin || dj < -kEpsin) {
     // plane-wave operators, _fteik2d.py:121-142
-    if (tv <= te + o.dx * vref && te <= tv + o.dz * vref && te >= tev && tv >= tev) {
+    if (fle(tv, te + o.dx * vref) && fle(te, tv + o.dz * vref) && fle(tev, te) &&
+        fle(tev, tv)) {
       const double ta = tev + te - tv;
       const double tb = tev - te + tv;
       const double d = ta - tb;
       t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(times4(vref * vref) * o.s2 - o.p2 * (d * d)),
                    o.r2);
-    } else if (te - tev <= div_by(o.dzz * vref, o.rhyp) && te - tev > 0.0) {
-      const double q = div_by(te - tev, o.rdz);
-      t2d = te + o.dx * sqrt(vref * vref - q * q);
-    } else if (tv - tev <= div_by(o.dxx * vref, o.rhyp) && tv - tev > 0.0) {
-      const double q = div_by(tv - tev, o.rdx);
-      t2d = tv + o.dz * sqrt(vref * vref - q * q);
+    } else if (fle(te - tev, div_by(o.dzz * vref, o.rhyp)) && flt(0.0, te - tev)) {
+      const double r = div_by(te - tev, o.rdz);
+      t2d = te + o.dx * sqrt(vref * vref - r * r);
+    } else if (fle(tv - tev, div_by(o.dxx * vref, o.rhyp)) && flt(0.0, tv - tev)) {
+      const double r = div_by(tv - tev, o.rdx);
+      t2d = tv + o.dz * sqrt(vref * vref - r * r);
     }
   } else {
     // spherical (factored) operator near the source, _fteik2d.py:144-171
-    if (tv < te + o.dx * vref && te < tv + o.dz * vref && te >= tev && tv >= tev) {
+    if (flt(tv, te + o.dx * vref) && flt(te, tv + o.dz * vref) && fle(tev, te) &&
+        fle(tev, tv)) {
       double tzc, txc;
       const double t0c = t_anad2(i, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero, tzc, txc);
       const double tauv = tv - t_ana2(i - sgntz, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
@@ -138,28 +160,52 @@ __device__ __forceinline__ void node_update2d(double* tt, uint8_t* rec, const do
       const double tauev = tev - t_ana2(i - sgntz, j - sgntx, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
       t2d = delta2(t2d, tauv, taue, tauev, t0c, tzc, txc, o.dzi, o.dxi, o.dz2i, o.dx2i,
                    sp.vzero, vref, sgntz, sgntx);
-      if (t2d < tv || t2d < te) t2d = kBig;
+      if (flt(t2d, tv) || flt(t2d, te)) t2d = kBig;
     }
   }
-  const double t0 = tt[n];
+  const double t0 = q.t0;
   // min(t0, t1d, t2d) with Python's semantics: keep the earlier argument
   // unless a later one compares strictly smaller.
   double tnew = t0;
-  if (t1d < tnew) tnew = t1d;
-  if (t2d < tnew) tnew = t2d;
-  if (!(tnew == t0)) {
+  if (flt(t1d, tnew)) tnew = t1d;
+  if (flt(t2d, tnew)) tnew = t2d;
+  if (!feq(tnew, t0)) {
     tt[n] = tnew;
     if (GRAD) {
       int a, b;
-      if (tnew == t1d1) {
+      if (feq(tnew, t1d1)) {
         a = sgntz; b = 0;
-      } else if (tnew == t1d2) {
+      } else if (feq(tnew, t1d2)) {
         a = 0; b = sgntx;
       } else {
         a = sgntz; b = sgntx;
       }
       rec[n] = (uint8_t)((a + 1) * 3 + (b + 1));
     }
+  }
+  return tnew;
+}
+
+// One pass over column j, rows i0, i0 + step, ..., i1 (inclusive), in the
+// reference's order.  Only tv depends on the previous node; every other
+// input of the next node is read while the current one is computed (the
+// previous column is complete, and this column's old values were written by
+// earlier passes), so the pass runs at the latency of the arithmetic chain.
+template <bool GRAD>
+__device__ __forceinline__ void column_pass2d(double* tt, uint8_t* rec, const double* slow,
+                                              const Ops2& o, const Source2& sp, int j, int i0,
+                                              int i1, int sgnvz, int sgnvx, int sgntz,
+                                              int sgntx, int NZ, int NX) {
+  const int step = sgntz;  // passes run in the direction of their upwind sign
+  double tv = tt[(long long)(i0 - sgntz) * NX + j];
+  In2 cur = load_in2(tt, slow, i0, j, sgnvz, sgnvx, sgntz, sgntx, NZ, NX);
+  for (int i = i0;; i += step) {
+    const bool more = i != i1;
+    In2 nxt;
+    if (more) nxt = load_in2(tt, slow, i + step, j, sgnvz, sgnvx, sgntz, sgntx, NZ, NX);
+    tv = node_update2d<GRAD>(tt, rec, o, sp, i, j, sgntz, sgntx, NX, tv, cur);
+    if (!more) break;
+    cur = nxt;
   }
 }
 
@@ -347,14 +393,12 @@ __global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const d
 
   for (int sw = 0; sw < nsweep; ++sw) {
     for (int j = 1; j < NX; ++j) {
-      for (int i = 1; i < NZ; ++i) node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 1, 1, 1, 1, NZ, NX);
-      for (int i = NZ - 2; i >= 0; --i)
-        node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 0, 1, -1, 1, NZ, NX);
+      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX);
+      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX);
     }
     for (int j = NX - 2; j >= 0; --j) {
-      for (int i = 1; i < NZ; ++i) node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 1, 0, 1, -1, NZ, NX);
-      for (int i = NZ - 2; i >= 0; --i)
-        node_update2d<GRAD>(tt, rec, slow, o, sp, i, j, 0, 0, -1, -1, NZ, NX);
+      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX);
+      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX);
     }
   }
 }

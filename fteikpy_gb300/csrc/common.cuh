@@ -62,23 +62,6 @@ __device__ __forceinline__ double pmin(double a, double b) {
 __device__ __forceinline__ bool deq(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
 }
-// IEEE comparisons on the integer pipe, for code that must keep NaN
-// semantics (every comparison with a NaN is false, != is true): the 2D sweep.
-__device__ __forceinline__ bool nan_bits(long long b) {
-  return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
-}
-__device__ __forceinline__ bool flt(double a, double b) {
-  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-  return !nan_bits(x) && !nan_bits(y) && okey(a) < okey(b);
-}
-__device__ __forceinline__ bool fle(double a, double b) {
-  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-  return !nan_bits(x) && !nan_bits(y) && okey(a) <= okey(b);
-}
-__device__ __forceinline__ bool feq(double a, double b) {
-  const long long x = __double_as_longlong(a);
-  return !nan_bits(x) && x == __double_as_longlong(b);
-}
 
 // ---- exact power-of-two scalings ---------------------------------------------
 

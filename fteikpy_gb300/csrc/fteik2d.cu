@@ -85,7 +85,7 @@ __device__ double delta2(double t1, double tauv, double taue, double tauev, doub
                  4.0 * ((double)sgntx * txc * dxi * ta + (double)sgntz * tzc * dzi * tb) +
                  4.0 * (vzero * vzero - vref * vref);
   double dpoly = bpoly * bpoly - 4.0 * apoly * cpoly;
-  return fle(0.0, dpoly) ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
+  return dpoly >= 0.0 ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
 }
 
 // The inputs of one node update that do not depend on the previous node of
@@ -117,7 +117,9 @@ __device__ __forceinline__ In2 load_in2(const double* tt, const double* slow, in
 // pass) and the other inputs.  Comparisons are IEEE comparisons here (not
 // integer keys): after a source on the model's far boundary the reference's
 // first propagation can leave NaN in tt, and Python's comparison and min
-// semantics on NaN must be kept.  Returns the node's value after the update.
+// semantics on NaN must be kept (NaN-aware integer comparisons measured
+// slower on this one-thread chain).  Returns the node's value after the
+// update.
 template <bool GRAD>
 __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const Ops2& o,
                                                 const Source2& sp, int i, int j, int sgntz,
@@ -128,31 +130,29 @@ __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const 
   const double t1d1 = tv + o.dz * vref;
   vref = pmin(q.sx0, q.sx1);
   const double t1d2 = te + o.dx * vref;
-  const double t1d = flt(t1d2, t1d1) ? t1d2 : t1d1;
+  const double t1d = t1d2 < t1d1 ? t1d2 : t1d1;
 
   double t2d = kBig;
   vref = q.s2;
   const int di = i - sp.zsi, dj = j - sp.xsi;
   if (di > kEpsin || di < -kEpsin || dj > kEpsin || dj < -kEpsin) {
     // plane-wave operators, _fteik2d.py:121-142
-    if (fle(tv, te + o.dx * vref) && fle(te, tv + o.dz * vref) && fle(tev, te) &&
-        fle(tev, tv)) {
+    if (tv <= te + o.dx * vref && te <= tv + o.dz * vref && te >= tev && tv >= tev) {
       const double ta = tev + te - tv;
       const double tb = tev - te + tv;
       const double d = ta - tb;
       t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(times4(vref * vref) * o.s2 - o.p2 * (d * d)),
                    o.r2);
-    } else if (fle(te - tev, div_by(o.dzz * vref, o.rhyp)) && flt(0.0, te - tev)) {
+    } else if (te - tev <= div_by(o.dzz * vref, o.rhyp) && te - tev > 0.0) {
       const double r = div_by(te - tev, o.rdz);
       t2d = te + o.dx * sqrt(vref * vref - r * r);
-    } else if (fle(tv - tev, div_by(o.dxx * vref, o.rhyp)) && flt(0.0, tv - tev)) {
+    } else if (tv - tev <= div_by(o.dxx * vref, o.rhyp) && tv - tev > 0.0) {
       const double r = div_by(tv - tev, o.rdx);
       t2d = tv + o.dz * sqrt(vref * vref - r * r);
     }
   } else {
     // spherical (factored) operator near the source, _fteik2d.py:144-171
-    if (flt(tv, te + o.dx * vref) && flt(te, tv + o.dz * vref) && fle(tev, te) &&
-        fle(tev, tv)) {
+    if (tv < te + o.dx * vref && te < tv + o.dz * vref && te >= tev && tv >= tev) {
       double tzc, txc;
       const double t0c = t_anad2(i, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero, tzc, txc);
       const double tauv = tv - t_ana2(i - sgntz, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
@@ -160,22 +160,22 @@ __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const 
       const double tauev = tev - t_ana2(i - sgntz, j - sgntx, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
       t2d = delta2(t2d, tauv, taue, tauev, t0c, tzc, txc, o.dzi, o.dxi, o.dz2i, o.dx2i,
                    sp.vzero, vref, sgntz, sgntx);
-      if (flt(t2d, tv) || flt(t2d, te)) t2d = kBig;
+      if (t2d < tv || t2d < te) t2d = kBig;
     }
   }
   const double t0 = q.t0;
   // min(t0, t1d, t2d) with Python's semantics: keep the earlier argument
   // unless a later one compares strictly smaller.
   double tnew = t0;
-  if (flt(t1d, tnew)) tnew = t1d;
-  if (flt(t2d, tnew)) tnew = t2d;
-  if (!feq(tnew, t0)) {
+  if (t1d < tnew) tnew = t1d;
+  if (t2d < tnew) tnew = t2d;
+  if (!(tnew == t0)) {
     tt[n] = tnew;
     if (GRAD) {
       int a, b;
-      if (feq(tnew, t1d1)) {
+      if (tnew == t1d1) {
         a = sgntz; b = 0;
-      } else if (feq(tnew, t1d2)) {
+      } else if (tnew == t1d2) {
         a = 0; b = sgntx;
       } else {
         a = sgntz; b = sgntx;

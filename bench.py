@@ -845,7 +845,9 @@ def main():
                 "what": "Eikonal3D(host velocity).solve(256 sources, gradients) + "
                         "raytrace and picks per source through the drop-in API",
             },
-            "gpu_launches": 7 * args.steps,
+            # per step: pencil order, coefficients, fill, init, sweep and gradient
+            # kernels of the solve, then the ray and ray-pack kernels
+            "gpu_launches": 8 * args.steps,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -534,9 +534,9 @@ def run_config5(args):
     from fteikpy_gb300._solver import solve3d_device
     from oracle import oracle as O
 
-    shape = (96, 128, 128)
+    shape = (48, 64, 64) if args.small else (96, 128, 128)
     v0, vt = tomography_models(shape)
-    src = surface_sources(shape, n_side=8, seed=7)
+    src = surface_sources(shape, n_side=4 if args.small else 8, seed=7)
     rec = surface_receivers(shape, n=NREC, seed=11)
     dev = torch.device("cuda", 0)
     t_obs = fp.traveltimes(torch.tensor(vt, device=dev), D, src, rec, NSWEEP).detach()
@@ -618,7 +618,8 @@ def run_config5(args):
                             v0=v0, t_obs=t_obs_h, t_pred=T)
     print(json.dumps({
         "config": 5,
-        "metric": "adjoint d(loss)/d(velocity), 96x128x128, 64 sources x 400 receivers, nsweep=2",
+        "metric": "adjoint d(loss)/d(velocity), %dx%dx%d, %d sources x 400 receivers, nsweep=2"
+                  % (shape + (len(src),)),
         "value": fwd + bwd, "unit": "ms", "higher_is_better": False,
         "forward_plain_ms": plain, "forward_with_tape_ms": fwd, "adjoint_ms": bwd,
         "adjoint_over_forward": bwd / plain, "forward_plus_adjoint_over_forward": (fwd + bwd) / plain,
@@ -658,7 +659,8 @@ def main():
                     help="--config 5: save the gradient and the finite differences (.npz)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 192 sources on a 64x128x128 grid (1.7 GB of traveltimes, "
-                         "> L2; 108K items per sweep, so the same team kernel as the full step)")
+                         "> L2; 108K items per sweep, so the same team kernel as the full step); "
+                         "with --config 5: 16 sources on 48x64x64")
     args = ap.parse_args()
     if args.small:
         global SHAPE, NSRC

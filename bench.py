@@ -661,7 +661,16 @@ def main():
                     help="profiling case: 192 sources on a 64x128x128 grid (1.7 GB of traveltimes, "
                          "> L2; 108K items per sweep, so the same team kernel as the full step); "
                          "with --config 5: 16 sources on 48x64x64")
+    ap.add_argument("--option", action="append", default=[], metavar="NAME=VALUE",
+                    help="library tuning knob (fteik_set_option), e.g. adjoint_chunk=4; "
+                         "results are identical for every setting")
     args = ap.parse_args()
+    if args.option and args.impl != "reference":
+        from fteikpy_gb300 import _lib
+
+        for item in args.option:
+            name, value = item.split("=", 1)
+            _lib.check(_lib.load().fteik_set_option(name.encode(), int(value)), "option " + name)
     if args.small:
         global SHAPE, NSRC
         SHAPE, NSRC = (64, 128, 128), 192

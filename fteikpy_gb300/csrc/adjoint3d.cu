@@ -203,152 +203,257 @@ __device__ __forceinline__ int cell_slot(int i, int j, int k, int ci, int cj, in
   return a * 4 + b * 2 + c;
 }
 
-// One node of one sweep, in reverse.  In sweep e (signs sz, sx, sy) the node
-// at local coordinates (ii, jj, kk) was updated after every node of a smaller
-// ii + jj + kk; going back, its hyperplane runs after the planes above it.
-// The node first collects what its readers of this sweep sent it (they lie
-// downwind, on planes already done), then, if this sweep changed it,
-// linearises the operator at the values it read, sends the adjoint on to its
-// inputs, books the slowness term and restores its previous value.  Arrays
-// other threads write are read through L2 (ld.global.cg).
-__device__ __forceinline__ void reverse_node(const RevArgs& A, int e, int src, int ii, int jj,
-                                             int kk) {
-  const int dir = e & 7;
-  const int sz = dir < 4 ? 1 : -1, sx = (dir & 1) ? -1 : 1, sy = (dir & 2) ? -1 : 1;
-  const long long NXY = (long long)A.NX * A.NY;
-  const int i = sz > 0 ? ii : A.NZ - 1 - ii;
-  const int j = sx > 0 ? jj : A.NX - 1 - jj;
-  const int k = sy > 0 ? kk : A.NY - 1 - kk;
-  const long long n = (long long)i * NXY + (long long)j * A.NY + k;
-  const long long base = (long long)src * A.nodes;
-  const long long tbase = ((long long)e * A.nsrc + src) * A.nodes;
-  // All reads are issued before any is used, so their latencies overlap.
-  const int code = __ldg(A.tcode + tbase + n);
-  const double lam0 = __ldcg(A.lam + base + n);
-  long long m[kSlots];
-  int dcode[kSlots];
-#pragma unroll
-  for (int slot = 0; slot < kSlots; ++slot) {
-    const int bz = (slot + 1) >> 2, bx = ((slot + 1) >> 1) & 1, by = (slot + 1) & 1;
-    const int mi = i + bz * sz, mj = j + bx * sx, mk = k + by * sy;
-    const bool in = mi >= 0 && mi < A.NZ && mj >= 0 && mj < A.NX && mk >= 0 && mk < A.NY;
-    m[slot] = (long long)mi * NXY + (long long)mj * A.NY + mk;
-    dcode[slot] = in ? (int)__ldg(A.tcode + tbase + m[slot]) : 255;
-  }
-  double part[kSlots];
-#pragma unroll
-  for (int slot = 0; slot < kSlots; ++slot) {
-    const int bz = (slot + 1) >> 2, bx = ((slot + 1) >> 1) & 1, by = (slot + 1) & 1;
-    part[slot] = 0.0;
-    if (dcode[slot] == 255) continue;
-    int az, ax, ay;
-    decode(dcode[slot], az, ax, ay);
-    if ((bz && !az) || (bx && !ax) || (by && !ay)) continue;
-    part[slot] = __ldcg(A.contrib + (base + m[slot]) * kSlots + slot);
-  }
-  double lam = lam0;
-  bool pulled = false;
-#pragma unroll
-  for (int slot = 0; slot < kSlots; ++slot) {
-    if (dcode[slot] == 255) continue;
-    lam += part[slot];
-    pulled = true;
-  }
-  if (code == 255) {
-    if (pulled) A.lam[base + n] = lam;
-    return;
-  }
-  int az, ax, ay;
-  decode(code, az, ax, ay);
-  double w[kSlots], ps;
-  int cell[4], ncell;
-  linearize(az, ax, ay, i, j, k, n, A.tt + base, A.slow, A.nz, A.nx, A.ny, A.NX, A.NY, A.o, w, ps,
-            cell, ncell);
-  double* c = A.contrib + (base + n) * kSlots;
-#pragma unroll
-  for (int slot = 0; slot < kSlots; ++slot) c[slot] = lam * w[slot];
-  for (int q = 0; q < ncell; ++q) {
-    const int ci = cell[q] / (A.nx * A.ny), cj = (cell[q] / A.ny) % A.nx, ck = cell[q] % A.ny;
-    double* g = A.g8 + (base + n) * 8 + cell_slot(i, j, k, ci, cj, ck);
-    *g = __ldcg(g) + lam * ps;
-  }
-  A.lam[base + n] = 0.0;
-  A.tt[base + n] = __ldg(A.told + tbase + n);
-}
+// The reverse pass.  Undoing sweep e (signs sz, sx, sy) must visit a node
+// after every node that read it in that sweep (its downwind neighbours n +
+// (bz*sz, bx*sx, by*sy)), so it is itself a directional sweep, against the
+// direction of e, and runs in the forward kernel's schedule with the signs
+// reversed: one warp owns one pencil of 4 x 8 node columns, lane (lj, lk)
+// handles row r = s - lj - lk at step s, and the pencils of all sources and
+// all sweeps run in one persistent launch, taking work items from a ticket
+// counter and waiting (bounded) on per-pencil progress counters.
+//
+// Each node n first pulls what its readers of the sweep sent it.  The reader
+// across input slot (bz, bx, by) lies in lane (lj - bx, lk - by) and was
+// visited bz + bx + by steps earlier, so inside a pencil the contribution
+// arrives by a warp shuffle from a short per-slot history kept in registers;
+// a reader in a neighbouring pencil left it in `contrib` (the lanes on a
+// pencil's far faces write the slots their neighbours consume).  A reader
+// that did not change in the sweep, or whose operator does not use the slot,
+// sends -0.0, which leaves the sum bit for bit unchanged.  Then, if the sweep
+// changed n, it recomputes its operator's partials from the values it read
+// (its upwind neighbours, not yet restored: they come later in this order),
+// forms what it sends to each input, books the slowness term and restores
+// its previous value.
+constexpr int kRevPW = 4;     // pencil width along j (the pencil is 4 x 8 columns)
+constexpr int kRevWarps = 4;  // warps per block
 
-// Barrier of the `nblocks` blocks of one group of a cooperative launch
-// (every block is resident). The last block to arrive resets the count and
-// publishes a new generation; the others poll the generation at most
-// spin_limit times, then flag FTEIK_DEVICE_WAIT_TIMEOUT and return false, as
-// they do once any block has flagged a failure.
-struct GridBarrier {
-  unsigned count, gen;
+struct RevSched {
+  unsigned* progress;  // [nsrc][PJ*PK]
+  unsigned* ticket;
+  int* status;
+  int PJ, PK, T, nepochs, chunk;
+  unsigned stride;  // progress counter range of one reverse sweep (>= T)
+  long long spin_limit;
 };
 
-__device__ bool group_barrier(GridBarrier* b, unsigned nblocks, int* status,
-                              long long spin_limit) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned g = ld_acquire(&b->gen);
-    __threadfence();
-    if (atomicAdd(&b->count, 1u) + 1u == nblocks) {
-      b->count = 0;
-      __threadfence();
-      st_release(&b->gen, g + 1u);
-    } else {
-      for (long long it = 0; ld_acquire(&b->gen) == g; ++it) {
-        if (it >= spin_limit) {
-          atomicCAS(status, 0, (int)kDeviceWaitTimeout);
-          ok = 0;
-          break;
-        }
-        if ((it & 15) == 15 && *((volatile int*)status) != 0) {
-          ok = 0;
-          break;
-        }
-        if (it >= 64) __nanosleep(64);
-      }
+// The p-th pencil in order of its diagonal JL + KL (then JL): every pencil a
+// pencil depends on in the same sweep comes first.
+__device__ __forceinline__ void pencil_at(int p, int PJ, int PK, int& JL, int& KL) {
+  for (int d = 0;; ++d) {
+    const int lo = imax(0, d - PK + 1), hi = imin(d, PJ - 1);
+    const int cnt = hi - lo + 1;
+    if (p < cnt) {
+      JL = lo + p;
+      KL = d - JL;
+      return;
     }
-    __threadfence();
-    ok_s = ok;
+    p -= cnt;
   }
-  __syncthreads();
-  return ok_s != 0;
 }
 
-// Every sweep in reverse, hyperplane by hyperplane, in one cooperative
-// launch. Sources are independent, so the blocks form `ngroups` groups that
-// each take every ngroups-th source and meet only at their own barrier: per
-// plane, the group's threads share out the plane's nodes (per column jj, the
-// band of kk whose ii = h - jj - kk lies in the grid), then wait for each
-// other before the plane below.
-__global__ void __launch_bounds__(256)
-    adj_reverse_kernel(const RevArgs A, int nepochs, int ngroups, GridBarrier* bars,
-                       int* status, long long spin_limit) {
-  const int hmax = A.NZ + A.NX + A.NY - 3;
-  const int g = (int)((long long)blockIdx.x * ngroups / gridDim.x);
-  const int b0 = (int)(((long long)g * gridDim.x + ngroups - 1) / ngroups);
-  const int b1 = (int)(((long long)(g + 1) * gridDim.x + ngroups - 1) / ngroups);
-  const unsigned nb = (unsigned)(b1 - b0);
-  const long long tid = (long long)(blockIdx.x - b0) * blockDim.x + threadIdx.x;
-  const long long nthreads = (long long)nb * blockDim.x;
-  GridBarrier* bar = bars + g;
-  for (int src = g; src < A.nsrc; src += ngroups) {
-    for (int e = nepochs - 1; e >= 0; --e) {
-      for (int h = hmax; h >= 0; --h) {
-        const int jlo = imax(0, h - (A.NZ - 1) - (A.NY - 1)), jhi = imin(A.NX - 1, h);
-        const int W = imin(imin(A.NZ, A.NY), h + 1);
-        const long long total = (long long)(jhi - jlo + 1) * W;
-        for (long long q = tid; q < total; q += nthreads) {
-          const int jj = jlo + (int)(q / W);
-          const int kk = imax(0, h - jj - (A.NZ - 1)) + (int)(q % W);
-          if (kk > imin(A.NY - 1, h - jj)) continue;
-          reverse_node(A, e, src, h - jj - kk, jj, kk);
+// Whether the operator with signs (az, ax, ay) reads input slot (bz, bx, by).
+__device__ __forceinline__ bool uses_slot(int az, int ax, int ay, int bz, int bx, int by) {
+  return !((bz && !az) || (bx && !ax) || (by && !ay));
+}
+
+template <int PW>
+__global__ void __launch_bounds__(kRevWarps * 32)
+    adj_sweep_kernel(const __grid_constant__ RevArgs A, const __grid_constant__ RevSched S) {
+  constexpr int PJW = PW, PKW = 32 / PW, LAG = PJW + PKW - 2;
+  const int lane = threadIdx.x & 31;
+  const int lj = lane / PKW, lk = lane % PKW;
+  const unsigned npen = (unsigned)S.PJ * S.PK;
+  const unsigned per_epoch = npen * (unsigned)A.nsrc;
+  const unsigned total_items = (unsigned)S.nepochs * per_epoch;
+  const unsigned cmask = (unsigned)S.chunk - 1u;
+  const long long NXY = (long long)A.NX * A.NY;
+  const double nz0 = -0.0;
+
+  for (;;) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(S.ticket, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= total_items) break;
+    const int er = (int)(t / per_epoch);  // sweeps are undone last first
+    const int e = S.nepochs - 1 - er;
+    const unsigned rem = t - (unsigned)er * per_epoch;
+    const int p = (int)(rem / (unsigned)A.nsrc);
+    const int src = (int)(rem - (unsigned)p * A.nsrc);
+    int JL, KL;
+    pencil_at(p, S.PJ, S.PK, JL, KL);
+    const int dir = e & 7;
+    const int sz = dir < 4 ? 1 : -1, sx = (dir & 1) ? -1 : 1, sy = (dir & 2) ? -1 : 1;
+    const int rz = -sz, rx = -sx, ry = -sy;  // direction of the reverse pass
+    const int J = rx > 0 ? JL : S.PJ - 1 - JL;
+    const int K = ry > 0 ? KL : S.PK - 1 - KL;
+    unsigned* prog = S.progress + (long long)src * npen;
+    unsigned* my_prog = prog + J * S.PK + K;
+    const unsigned base = (unsigned)er * S.stride;
+
+    // The previous reverse sweep must be done on this pencil and its 8
+    // neighbours: their nodes are restored to the values this sweep's
+    // operators read, and their readers have consumed the contributions this
+    // pencil is about to overwrite.
+    bool ok = true;
+    if (lane == 0 && er > 0) {
+      const unsigned done = base - S.stride + (unsigned)S.T;
+      for (int dj = -1; dj <= 1 && ok; ++dj)
+        for (int dk = -1; dk <= 1 && ok; ++dk) {
+          const int J2 = J + dj, K2 = K + dk;
+          if (J2 < 0 || J2 >= S.PJ || K2 < 0 || K2 >= S.PK) continue;
+          ok = wait_geq(prog + J2 * S.PK + K2, done, S.status, S.spin_limit);
         }
-        if (!group_barrier(bar, nb, status, spin_limit)) return;
+      if (ok) __threadfence();
+    }
+    ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    if (!ok) {
+      __syncwarp();
+      if (lane == 0) st_release(my_prog, base + (unsigned)S.T);
+      continue;
+    }
+
+    // Pencils upstream in the reverse direction hold the readers across the
+    // pencil's near faces.
+    const int Ju = J - rx, Ku = K - ry;
+    const bool hJu = Ju >= 0 && Ju < S.PJ, hKu = Ku >= 0 && Ku < S.PK;
+    const unsigned* prog_j = prog + Ju * S.PK + K;
+    const unsigned* prog_k = prog + J * S.PK + Ku;
+    const unsigned* prog_jk = prog + Ju * S.PK + Ku;
+
+    const int j = rx > 0 ? J * PJW + lj : J * PJW + (PJW - 1) - lj;
+    const int k = ry > 0 ? K * PKW + lk : K * PKW + (PKW - 1) - lk;
+    const bool in_grid = j < A.NX && k < A.NY;
+    // readers along j and k exist (the reader along i exists from row 1 on)
+    const bool jin = j + sx >= 0 && j + sx < A.NX, kin = k + sy >= 0 && k + sy < A.NY;
+    const long long di = (long long)sz * NXY, dj = (long long)sx * A.NY, dk = sy;
+    const long long jk = (long long)j * A.NY + k;
+    const long long sbase = (long long)src * A.nodes;
+    const long long tbase = ((long long)e * A.nsrc + src) * A.nodes;
+    double* lam_s = A.lam + sbase;
+    double* tt_s = A.tt + sbase;
+    double* con_s = A.contrib + sbase * kSlots;
+    double* g8_s = A.g8 + sbase * 8;
+    const uint8_t* code_s = A.tcode + tbase;
+    const double* old_s = A.told + tbase;
+    const bool face_j = lj == PJW - 1, face_k = lk == PKW - 1;
+
+    // What this lane sent across each slot 1, 2 and 3 steps ago.
+    double h0 = nz0, h1 = nz0, h3 = nz0;                         // slots 0, 1, 3
+    double h2a = nz0, h2b = nz0, h4a = nz0, h4b = nz0, h5a = nz0, h5b = nz0;  // 2, 4, 5
+    double h6a = nz0, h6b = nz0, h6c = nz0;                      // slot 6
+    for (int s = 0; s < S.T; ++s) {
+      if (((unsigned)s & cmask) == 0) {
+        const int last = imin(s + (int)cmask, S.T - 1);
+        bool w = true;
+        if (lane == 0) {
+          if (hJu) w = wait_geq(prog_j, base + (unsigned)imin(last + PJW, S.T), S.status, S.spin_limit);
+          if (w && hKu)
+            w = wait_geq(prog_k, base + (unsigned)imin(last + PKW, S.T), S.status, S.spin_limit);
+          if (w && hJu && hKu)
+            w = wait_geq(prog_jk, base + (unsigned)imin(last + LAG + 1, S.T), S.status,
+                         S.spin_limit);
+          if (w) __threadfence();
+        }
+        w = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
+        __syncwarp();
+        if (!w) break;
       }
+      // Contributions from readers in this pencil (lane (lj-bx, lk-by),
+      // bz+bx+by steps ago); lanes on the near faces replace them below.
+      double p0 = __shfl_up_sync(0xffffffffu, h0, 1);
+      double p1 = __shfl_up_sync(0xffffffffu, h1, PKW);
+      double p2 = __shfl_up_sync(0xffffffffu, h2b, PKW + 1);
+      const double p3 = h3;
+      double p4 = __shfl_up_sync(0xffffffffu, h4b, 1);
+      double p5 = __shfl_up_sync(0xffffffffu, h5b, PKW);
+      double p6 = __shfl_up_sync(0xffffffffu, h6c, PKW + 1);
+      const int r = s - lj - lk;
+      const bool act = in_grid && r >= 0 && r < A.NZ;
+      double c[kSlots];
+#pragma unroll
+      for (int q = 0; q < kSlots; ++q) c[q] = nz0;
+      if (act) {
+        const int i = rz > 0 ? r : A.NZ - 1 - r;
+        const long long n = (long long)i * NXY + jk;
+        const int code = __ldg(code_s + n);
+        const double lam0 = __ldcg(lam_s + n);
+        const bool iin = r > 0;
+        if (lj == 0) {
+          p1 = jin ? __ldcg(con_s + (n + dj) * kSlots + 1) : nz0;
+          p5 = jin && iin ? __ldcg(con_s + (n + di + dj) * kSlots + 5) : nz0;
+        }
+        if (lk == 0) {
+          p0 = kin ? __ldcg(con_s + (n + dk) * kSlots + 0) : nz0;
+          p4 = kin && iin ? __ldcg(con_s + (n + di + dk) * kSlots + 4) : nz0;
+        }
+        if (lj == 0 || lk == 0) {
+          p2 = jin && kin ? __ldcg(con_s + (n + dj + dk) * kSlots + 2) : nz0;
+          p6 = jin && kin && iin ? __ldcg(con_s + (n + di + dj + dk) * kSlots + 6) : nz0;
+        }
+        double lam = lam0 + p0;
+        lam = lam + p1;
+        lam = lam + p2;
+        lam = lam + p3;
+        lam = lam + p4;
+        lam = lam + p5;
+        lam = lam + p6;
+        if (code == 255) {
+          if (__double_as_longlong(lam) != __double_as_longlong(lam0)) lam_s[n] = lam;
+        } else {
+          int az, ax, ay;
+          decode(code, az, ax, ay);
+          double w[kSlots], ps;
+          int cell[4], ncell;
+          linearize(az, ax, ay, i, j, k, n, tt_s, A.slow, A.nz, A.nx, A.ny, A.NX, A.NY, A.o, w,
+                    ps, cell, ncell);
+#pragma unroll
+          for (int q = 0; q < kSlots; ++q) {
+            const int bz = (q + 1) >> 2, bx = ((q + 1) >> 1) & 1, by = (q + 1) & 1;
+            if (uses_slot(az, ax, ay, bz, bx, by)) c[q] = lam * w[q];
+          }
+          for (int q = 0; q < ncell; ++q) {
+            const int ci = cell[q] / (A.nx * A.ny), cj = (cell[q] / A.ny) % A.nx,
+                      ck = cell[q] % A.ny;
+            double* g = g8_s + n * 8 + cell_slot(i, j, k, ci, cj, ck);
+            *g = __ldcg(g) + lam * ps;
+          }
+          lam_s[n] = 0.0;
+          tt_s[n] = __ldg(old_s + n);
+        }
+        // Slots read by the readers' pencils across the far faces.
+        double* co = con_s + n * kSlots;
+        if (face_j) {
+          co[1] = c[1];
+          co[5] = c[5];
+        }
+        if (face_k) {
+          co[0] = c[0];
+          co[4] = c[4];
+        }
+        if (face_j || face_k) {
+          co[2] = c[2];
+          co[6] = c[6];
+        }
+      }
+      h0 = c[0];
+      h1 = c[1];
+      h3 = c[3];
+      h2b = h2a; h2a = c[2];
+      h4b = h4a; h4a = c[4];
+      h5b = h5a; h5a = c[5];
+      h6c = h6b; h6b = h6a; h6a = c[6];
+      if (((unsigned)(s + 1) & cmask) == 0 || s + 1 == S.T) {
+        __syncwarp();
+        if (lane == 0) {
+          __threadfence();
+          st_release(my_prog, base + (unsigned)(s + 1));
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence();
+      st_release(my_prog, base + (unsigned)S.T);
     }
   }
 }
@@ -461,11 +566,14 @@ __global__ void adj_gather_kernel(const RevArgs A, const double* vzg, double* gr
 
 struct AdjLayout {
   size_t tt, lam, contrib, g8, vzg, sync, total;
+  int PJ, PK;
 };
 
 static AdjLayout adj_layout(int nz, int nx, int ny, int nsrc) {
   const size_t N = (size_t)(nz + 1) * (nx + 1) * (ny + 1) * nsrc;
   AdjLayout L;
+  L.PJ = (nx + 1 + kRevPW - 1) / kRevPW;
+  L.PK = (ny + 1 + 32 / kRevPW - 1) / (32 / kRevPW);
   size_t off = 0;
   L.tt = off;
   off = align_up(off + 8 * N);
@@ -477,8 +585,8 @@ static AdjLayout adj_layout(int nz, int nx, int ny, int nsrc) {
   off = align_up(off + 8 * 8 * N);
   L.vzg = off;
   off = align_up(off + 8 * (size_t)nsrc);
-  L.sync = off;  // int status, then one barrier per source group
-  off = align_up(off + 8 + 8 * (size_t)nsrc);
+  L.sync = off;  // int status, unsigned ticket, then the progress counters
+  off = align_up(off + 8 + 4 * (size_t)L.PJ * L.PK * nsrc);
   L.total = off;
   return L;
 }
@@ -540,19 +648,28 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
   adj_seed_kernel<<<(nsrc + 63) / 64, 64, 0, st>>>(A, ax0, ax1, ax2, sources, receivers, nrec,
                                                    grad_tt_rec, vzg);
   FTEIK_CHECK(cudaGetLastError());
-  int nepochs = 8 * nsweep;
+  const int nepochs = 8 * nsweep;
+  int* status = (int*)(ws + L.sync);
   if (nepochs > 0) {
-    int* status = (int*)(ws + L.sync);
-    GridBarrier* bars = (GridBarrier*)(ws + L.sync + 8);
-    FTEIK_CHECK(cudaMemsetAsync(ws + L.sync, 0, 8 + sizeof(GridBarrier) * (size_t)nsrc, st));
-    const void* kern = (const void*)adj_reverse_kernel;
-    const int blocks = resident_blocks(kern, 256);
-    // one group of blocks per source while there are blocks enough
-    int ngroups = std::min(nsrc, blocks);
-    long long limit = spin_limit > 0 ? spin_limit : (1LL << 25);
-    void* args[] = {(void*)&A,    (void*)&nepochs, (void*)&ngroups,
-                    (void*)&bars, (void*)&status,  (void*)&limit};
-    FTEIK_CHECK(cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(256), args, 0, st));
+    RevSched R;
+    R.status = status;
+    R.ticket = (unsigned*)(ws + L.sync + 4);
+    R.progress = (unsigned*)(ws + L.sync + 8);
+    R.PJ = L.PJ;
+    R.PK = L.PK;
+    R.T = A.NZ + kRevPW + 32 / kRevPW - 2;
+    R.nepochs = nepochs;
+    const long long chunk = option_value(kOptAdjointChunk);
+    R.chunk = chunk > 0 ? (int)chunk : 4;  // 4 measured best on 96x128x128, 64 sources
+    R.stride = (unsigned)R.T;
+    R.spin_limit = spin_limit > 0 ? spin_limit : (1LL << 25);
+    FTEIK_CHECK(
+        cudaMemsetAsync(ws + L.sync, 0, 8 + 4 * (size_t)L.PJ * L.PK * nsrc, st));
+    // persistent: as many blocks as are resident at once, so every ticket
+    // holder runs and each wait is on an item that is already running
+    const int threads = kRevWarps * 32;
+    const int blocks = resident_blocks((const void*)adj_sweep_kernel<kRevPW>, threads);
+    adj_sweep_kernel<kRevPW><<<blocks, threads, 0, st>>>(A, R);
   }
   FTEIK_CHECK(cudaGetLastError());
   adj_initial_kernel<<<(nsrc * 8 + 127) / 128, 128, 0, st>>>(A);
@@ -561,7 +678,7 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
   FTEIK_CHECK(cudaStreamSynchronize(st));
   if (nepochs > 0) {
     int dev_status = 0;
-    FTEIK_CHECK(cudaMemcpy(&dev_status, ws + L.sync, sizeof(int), cudaMemcpyDeviceToHost));
+    FTEIK_CHECK(cudaMemcpy(&dev_status, status, sizeof(int), cudaMemcpyDeviceToHost));
     if (dev_status != 0) return dev_status;
   }
   return kOk;

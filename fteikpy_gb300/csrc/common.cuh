@@ -116,6 +116,22 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Lane-0 bounded wait until *p >= target.  Gives up (and flags the status)
+// after spin_limit polls, or as soon as another warp has flagged a failure.
+__device__ __forceinline__ bool wait_geq(const unsigned* p, unsigned target, int* status,
+                                         long long spin_limit) {
+  if (ld_acquire(p) >= target) return true;
+  for (long long it = 0;; ++it) {
+    __nanosleep(it < 8 ? 64 : 512);
+    if (ld_acquire(p) >= target) return true;
+    if (it >= spin_limit) {
+      atomicCAS(status, 0, (int)kDeviceWaitTimeout);
+      return false;
+    }
+    if ((it & 15) == 15 && *((volatile int*)status) != 0) return false;
+  }
+}
+
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));

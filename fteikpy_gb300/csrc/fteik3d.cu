@@ -283,22 +283,6 @@ struct Sweep3Args {
   long long spin_limit;
 };
 
-// Lane-0 bounded wait until *p >= target.  Gives up (and flags the status)
-// after spin_limit polls, or as soon as another warp has flagged a failure.
-__device__ __forceinline__ bool wait_geq(const unsigned* p, unsigned target, int* status,
-                                         long long spin_limit) {
-  if (ld_acquire(p) >= target) return true;
-  for (long long it = 0;; ++it) {
-    __nanosleep(it < 8 ? 64 : 512);
-    if (ld_acquire(p) >= target) return true;
-    if (it >= spin_limit) {
-      atomicCAS(status, 0, (int)kDeviceWaitTimeout);
-      return false;
-    }
-    if ((it & 15) == 15 && *((volatile int*)status) != 0) return false;
-  }
-}
-
 // The persistent sweep kernel.  PW is the pencil width along j (the pencil is
 // PW x 32/PW columns); MULTI takes items from the multi-model tables.
 template <bool GRAD, bool COEF, int PW, bool MULTI>

@@ -35,7 +35,8 @@ enum Option : int {
   kOptSweepChunk = 2,   // 3D steps between progress publications: 1, 2, 4, ... 64
   kOptKeepTest = 3,     // 3D unchanged-node test before the 2D/3D operators: 0 off
   kOptSweepTeam = 4,    // 3D team kernel (compacted operators): 1 on, 0 off
-  kOptCount = 5,
+  kOptAdjointChunk = 5, // adjoint reverse sweeps: steps between progress publications
+  kOptCount = 6,
 };
 long long option_value(int opt);
 

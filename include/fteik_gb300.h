@@ -50,7 +50,9 @@ int fteik_kernel_timing(int on);
  * solves with the team kernel (compacted operators; the default from 4
  * sources), 0 with one warp per pencil. "sweep_keep_test": 0 turns off the
  * test that skips the 2D/3D operators of nodes that provably keep their value
- * (grids with equal spacings only). Results are identical for every setting.
+ * (grids with equal spacings only). "adjoint_chunk": steps between progress
+ * publications of the adjoint's reverse pass, a power of 2 up to 64.
+ * Results are identical for every setting.
  * fteik_get_option reads a knob back. */
 int fteik_set_option(const char* name, long long value);
 int fteik_get_option(const char* name, long long* value);
@@ -200,10 +202,11 @@ int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny, double dz,
  *  receivers   device [nrec][3], the same receivers for every source
  *  grad_tt_rec device [nsrc][nrec] d(loss)/d(traveltime at receiver)
  *  grad_slow   device [nz][nx][ny] d(loss)/d(slowness), summed over sources
- *  spin_limit  polls of one grid-barrier wait before the reverse pass gives
- *              up with FTEIK_DEVICE_WAIT_TIMEOUT (<= 0: default)
- * The reverse pass is one cooperative launch that visits every hyperplane of
- * every sweep. Deterministic (no floating-point atomics). Both calls block. */
+ *  spin_limit  polls of one progress wait before the reverse pass gives up
+ *              with FTEIK_DEVICE_WAIT_TIMEOUT (<= 0: default)
+ * The reverse pass undoes every sweep of every source in one persistent
+ * launch, as sweeps against the forward direction in the solve's pencil
+ * schedule. Deterministic (no floating-point atomics). Both calls block. */
 size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep);
 int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, double dz, double dx,
                        double dy, const double* sources, int nsrc, int nsweep, double* tt,

@@ -108,7 +108,7 @@ def test_adjoint_with_zero_sweeps_and_outside_receivers():
 
 
 def test_reverse_pass_wait_timeout_is_reported_and_recoverable(monkeypatch):
-    """The reverse pass's grid barrier waits at most spin_limit polls: with a
+    """The reverse pass's progress waits poll at most spin_limit times: with a
     limit of 1 it reports a timeout instead of hanging, and the next backward
     on the same context gives the exact gradient."""
     from fteikpy_gb300 import _adjoint

@@ -148,3 +148,25 @@ def test_adjoint_through_either_sweep_kernel(team):
         assert np.abs(g - go).max() <= 1e-12 * np.abs(go).max()
     finally:
         lib.fteik_set_option(b"sweep_team", -1)
+
+
+def test_reverse_pass_chunk_does_not_change_the_gradient():
+    """The reverse pass publishes its progress every `adjoint_chunk` steps;
+    the schedule changes, the gradient's bits do not."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    shape, nsweep = (13, 17, 22), 2
+    src, rec = geometry(shape, 5, 25, 9)
+    t_obs = oracle_times(velocity(shape, True), src, rec, nsweep)
+    v0 = velocity(shape, False)
+    grads = []
+    try:
+        for chunk in (1, 4, 64):
+            assert lib.fteik_set_option(b"adjoint_chunk", chunk) == 0
+            grads.append(gpu_gradient(v0, src, rec, nsweep, t_obs)[1])
+    finally:
+        lib.fteik_set_option(b"adjoint_chunk", -1)
+    assert all(np.array_equal(grads[0], g) for g in grads[1:])
+    go = oracle_velocity_gradient(v0, src, rec, nsweep, t_obs)
+    assert np.abs(grads[0] - go).max() <= 1e-12 * np.abs(go).max()

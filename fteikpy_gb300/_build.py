@@ -32,6 +32,11 @@ NVCC_FLAGS = ARCH + [
     "-I" + CSRC,
 ]
 
+# Everything that reproduces the reference's arithmetic is compiled without
+# multiply-add contraction (bitwise parity). The adjoint's partials have no
+# such contract, so that file may contract.
+CONTRACTED = {"adjoint3d.cu"}
+
 
 def _nvcc():
     for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
@@ -69,7 +74,10 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        flags = NVCC_FLAGS
+        if os.path.basename(src) in CONTRACTED:
+            flags = [f for f in flags if not f.startswith("--fmad")] + ["--fmad=true"]
+        cmd = [nvcc] + flags + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         res = subprocess.run(cmd, capture_output=True, text=True)

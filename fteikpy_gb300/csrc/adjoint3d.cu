@@ -17,6 +17,7 @@
 // Every transfer is a pull or a per-node accumulation, so the result is the
 // same from run to run.
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 
 #include "common.cuh"
@@ -50,117 +51,138 @@ __device__ __forceinline__ void decode(int code, int& az, int& ax, int& ay) {
   ay = code % 3 - 1;
 }
 
-// The distinct cells of the list whose slowness is minimal.  Boundary clamps
-// can list a cell twice; that is one cell, not a tie.
-__device__ __forceinline__ int min_cells(const double* slow, const int* cells, int n,
-                                         int (&out)[4], double& vmin) {
-  double bv = __ldg(slow + cells[0]);
-  for (int q = 1; q < n; ++q) bv = fmin(bv, __ldg(slow + cells[q]));
-  int m = 0;
-  for (int q = 0; q < n; ++q) {
-    if (__ldg(slow + cells[q]) != bv) continue;
-    bool seen = false;
-    for (int r = 0; r < m; ++r) seen = seen || out[r] == cells[q];
-    if (!seen) out[m++] = cells[q];
+// The cells around node (i, j, k) are named by their slot a*4 + b*2 + c:
+// a = 0 for the cell row max(i-1, 0), 1 for min(i, nz-1), and b, c likewise
+// along j and k; where the two rows coincide (the model's edges) the one cell
+// is slot a = 0.  CellFrame holds, per axis, the linear offsets of the two
+// rows and whether they differ.
+struct CellFrame {
+  long long z0, z1, x0, x1, y0, y1;  // row offsets into slow: z * nx * ny, x * ny, y
+  int za, xa, ya;                    // 1 if the second row is a different cell
+};
+
+__device__ __forceinline__ long long cell_at(const CellFrame& F, int slot) {
+  return ((slot & 4) ? F.z1 : F.z0) + ((slot & 2) ? F.x1 : F.x0) + ((slot & 1) ? F.y1 : F.y0);
+}
+
+// The distinct cells of the list whose slowness is minimal, as a bit mask
+// of slots (duplicate slots from collapsed rows are one cell, not a tie).
+// Slowness is positive, so its bit patterns order like its values.
+template <int N>
+__device__ __forceinline__ unsigned min_slots(const double* slow, const CellFrame& F,
+                                              const int (&slots)[N], double& vmin) {
+  long long bits[N];
+  long long bv = LLONG_MAX;
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    bits[q] = __double_as_longlong(__ldg(slow + cell_at(F, slots[q])));
+    bv = bits[q] < bv ? bits[q] : bv;
   }
-  vmin = bv;
-  return m;
+  unsigned mask = 0;
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    if (bits[q] == bv) mask |= 1u << slots[q];
+  vmin = __longlong_as_double(bv);
+  return mask;
 }
 
 // Partials of the operator that produced t_n (signs az, ax, ay from the
 // branch record) with respect to its inputs (slot (bz,bx,by) = input at
 // n - (bz*az, bx*ax, by*ay)) and to the slowness it used, evaluated at the
-// input values in t.  Recomputed from the traveltimes, _fteik3d.py:76-159.
-// The 1D and 2D operators use the minimum slowness of 4 or 2 cells.  Where
-// several cells share that minimum the solver has no derivative: lowering one
-// of them moves the result, raising it does not.  Each tied cell then gets
-// half the partial, the mean of its two one-sided derivatives, which is what
-// a central difference on that cell measures.  The cells are returned in
-// cells[0..ncell) with the partial ps for each.
+// input values in t: the derivatives of _fteik3d.py:76-159.  The 1D and 2D
+// operators use the minimum slowness of 4 or 2 cells.  Where several cells
+// share that minimum the solver has no derivative: lowering one of them moves
+// the result, raising it does not.  Each tied cell then gets half the
+// partial, the mean of its two one-sided derivatives, which is what a central
+// difference on that cell measures.  The cells come back as a bit mask of
+// slots, with the partial ps for each.
+//
+// These partials need not reproduce any rounding of the reference, so they
+// use the per-launch reciprocals of the operators' denominators and one
+// reciprocal square root per operator instead of divisions.
 __device__ void linearize(int az, int ax, int ay, int i, int j, int k, long long n,
-                          const double* t, const double* slow, int nz_, int nx_, int ny_,
-                          int NX_, int NY_, const Ops3& o, double (&w)[kSlots], double& ps,
-                          int (&cell)[4], int& ncell) {
-  struct Dims { int nz, nx, ny, NX, NY; } A{nz_, nx_, ny_, NX_, NY_};
+                          const double* t, const double* slow, const CellFrame& F, int NX_,
+                          int NY_, const Ops3& o, double (&w)[kSlots], double& ps,
+                          unsigned& cells) {
   const long long NXY = (long long)NX_ * NY_;
 #pragma unroll
   for (int e = 0; e < kSlots; ++e) w[e] = 0.0;
   ps = 0.0;
-  ncell = 0;
   double v;
-  const int im = imax(i - 1, 0), ip = imin(i, A.nz - 1);
-  const int jm = imax(j - 1, 0), jp = imin(j, A.nx - 1);
-  const int km = imax(k - 1, 0), kp = imin(k, A.ny - 1);
-  const int i1 = az > 0 ? i - 1 : i, j1 = ax > 0 ? j - 1 : j, k1 = ay > 0 ? k - 1 : k;
-#define C(a, b, c) (((a)*A.nx + (b)) * A.ny + (c))
-#define T(bz, bx, by) __ldcg(t + n - (long long)(bz) * az * NXY - (long long)(bx) * ax * A.NY - (by) * ay)
+  // upwind row of each axis: the reference's i1 = i - 1 (sign +) or i (sign -)
+  const int a1 = az > 0 ? 0 : F.za, b1 = ax > 0 ? 0 : F.xa, c1 = ay > 0 ? 0 : F.ya;
+#define T(bz, bx, by) \
+  __ldcg(t + n - (long long)(bz) * az * NXY - (long long)(bx) * ax * NY_ - (by) * ay)
   const int nnz = (az != 0) + (ax != 0) + (ay != 0);
   if (nnz == 1) {
-    int cells[4];
+    int sl[4];
     if (az != 0) {
-      cells[0] = C(i1, jm, km); cells[1] = C(i1, jm, kp); cells[2] = C(i1, jp, km); cells[3] = C(i1, jp, kp);
+      sl[0] = a1 * 4; sl[1] = a1 * 4 + F.ya; sl[2] = a1 * 4 + F.xa * 2; sl[3] = sl[2] + F.ya;
       w[3] = 1.0;
       ps = o.dz;
     } else if (ax != 0) {
-      cells[0] = C(im, j1, km); cells[1] = C(ip, j1, km); cells[2] = C(im, j1, kp); cells[3] = C(ip, j1, kp);
+      sl[0] = b1 * 2; sl[1] = F.za * 4 + b1 * 2; sl[2] = b1 * 2 + F.ya; sl[3] = sl[1] + F.ya;
       w[1] = 1.0;
       ps = o.dx;
     } else {
-      cells[0] = C(im, jm, k1); cells[1] = C(im, jp, k1); cells[2] = C(ip, jm, k1); cells[3] = C(ip, jp, k1);
+      sl[0] = c1; sl[1] = F.xa * 2 + c1; sl[2] = F.za * 4 + c1; sl[3] = sl[2] + F.xa * 2;
       w[0] = 1.0;
       ps = o.dy;
     }
-    ncell = min_cells(slow, cells, 4, cell, v);
+    cells = min_slots(slow, F, sl, v);
   } else if (nnz == 2) {
     // plane operators, _fteik3d.py:106-143
-    double c1, c2, ta, tb;
-    int cells[2], s1, s2, s12;
+    double c1v, c2v, iS, ta, tb;
+    int sl[2];
     if (ay == 0) {  // ZX: inputs tv (slot 3), te (1), tev (5)
       const double tv = T(1, 0, 0), te = T(0, 1, 0), tev = T(1, 1, 0);
       ta = tev + te - tv;
       tb = tev - te + tv;
-      c1 = o.dz2i; c2 = o.dx2i;  // num = tb*c1 + ta*c2
-      s1 = 3; s2 = 1; s12 = 5;
-      cells[0] = C(i1, j1, km); cells[1] = C(i1, j1, kp);
+      c1v = o.dz2i; c2v = o.dx2i; iS = o.rzx.hi;  // num = tb*c1 + ta*c2
+      sl[0] = a1 * 4 + b1 * 2; sl[1] = sl[0] + F.ya;
     } else if (ax == 0) {  // ZY: inputs tv (3), tn (0), tnv (4)
       const double tv = T(1, 0, 0), tn = T(0, 0, 1), tnv = T(1, 0, 1);
       ta = tv - tn + tnv;
       tb = tn - tv + tnv;
-      c1 = o.dz2i; c2 = o.dy2i;  // num = ta*c1 + tb*c2
-      s1 = 3; s2 = 0; s12 = 4;
-      cells[0] = C(i1, jm, k1); cells[1] = C(i1, jp, k1);
+      c1v = o.dz2i; c2v = o.dy2i; iS = o.rzy.hi;  // num = ta*c1 + tb*c2
+      sl[0] = a1 * 4 + c1; sl[1] = sl[0] + F.xa * 2;
     } else {  // XY: inputs te (1), tn (0), ten (2)
       const double te = T(0, 1, 0), tn = T(0, 0, 1), ten = T(0, 1, 1);
       ta = te - tn + ten;
       tb = tn - te + ten;
-      c1 = o.dx2i; c2 = o.dy2i;  // num = ta*c1 + tb*c2
-      s1 = 1; s2 = 0; s12 = 2;
-      cells[0] = C(im, j1, k1); cells[1] = C(ip, j1, k1);
+      c1v = o.dx2i; c2v = o.dy2i; iS = o.rxy.hi;  // num = ta*c1 + tb*c2
+      sl[0] = b1 * 2 + c1; sl[1] = sl[0] + F.za * 4;
     }
-    ncell = min_cells(slow, cells, 2, cell, v);
-    const double S = c1 + c2, d = ta - tb;
-    const double Q = 4.0 * v * v * S - c1 * c2 * d * d;
-    const double R = Q > 0.0 ? sqrt(Q) : 0.0;
-    const double r = R > 0.0 ? c1 * c2 * d / R : 0.0;
+    cells = min_slots(slow, F, sl, v);
+    const double S = c1v + c2v, d = ta - tb, p12 = c1v * c2v;
+    const double Q = 4.0 * v * v * S - p12 * d * d;
+    // t = (num + R) / S with R = sqrt(Q); only 1/R enters the partials
+    const double iR = Q > 0.0 ? rsqrt(Q) : 0.0;
+    const double r = p12 * d * iR;
     // partials of t with respect to ta and tb
     double dta, dtb;
     if (ay == 0) {  // num = tb*dz2i + ta*dx2i
-      dta = (c2 - r) / S;
-      dtb = (c1 + r) / S;
+      dta = (c2v - r) * iS;
+      dtb = (c1v + r) * iS;
     } else {  // num = ta*c1 + tb*c2
-      dta = (c1 - r) / S;
-      dtb = (c2 + r) / S;
+      dta = (c1v - r) * iS;
+      dtb = (c2v + r) * iS;
     }
     // ta = x12 + x2 - x1 (ZX: tev + te - tv) or x1 - x2 + x12 (ZY, XY)
     if (ay == 0) {
-      w[s1] = -dta + dtb;  // tv
-      w[s2] = dta - dtb;   // te
+      w[3] = dtb - dta;  // tv
+      w[1] = dta - dtb;  // te
+      w[5] = dta + dtb;  // tev
+    } else if (ax == 0) {
+      w[3] = dta - dtb;  // tv
+      w[0] = dtb - dta;  // tn
+      w[4] = dta + dtb;  // tnv
     } else {
-      w[s1] = dta - dtb;   // tv (ZY) / te (XY)
-      w[s2] = -dta + dtb;  // tn
+      w[1] = dta - dtb;  // te
+      w[0] = dtb - dta;  // tn
+      w[2] = dta + dtb;  // ten
     }
-    w[s12] = dta + dtb;
-    ps = R > 0.0 ? 4.0 * v / R : 0.0;  // dt/dv = (dR/dv) / S, dR/dv = 4 v S / R
+    ps = 4.0 * v * iR;  // dt/dv = (dR/dv) / S, dR/dv = 4 v S / R
   } else {
     // 3D operator, _fteik3d.py:145-159
     const double tv = T(1, 0, 0), te = T(0, 1, 0), tn = T(0, 0, 1), tev = T(1, 1, 0);
@@ -168,30 +190,30 @@ __device__ void linearize(int az, int ax, int ay, int i, int j, int k, long long
     const double ta = te - 0.5 * tn + 0.5 * ten - 0.5 * tv + 0.5 * tev - tnv + tnve;
     const double tb = tv - 0.5 * tn + 0.5 * tnv - 0.5 * te + 0.5 * tev - ten + tnve;
     const double tc = tn - 0.5 * te + 0.5 * ten - 0.5 * tv + 0.5 * tnv - tev + tnve;
-    cell[0] = C(i1, j1, k1);
-    ncell = 1;
-    v = __ldg(slow + cell[0]);
+    const int sl = a1 * 4 + b1 * 2 + c1;
+    cells = 1u << sl;
+    v = __ldg(slow + cell_at(F, sl));
+    const double dab = ta - tb, dbc = tb - tc, dac = ta - tc;
     const double t2 = v * v * o.dsum * 9.0;
-    const double t3 = o.dz2dx2 * (ta - tb) * (ta - tb) + o.dz2dy2 * (tb - tc) * (tb - tc) +
-                      o.dx2dy2 * (ta - tc) * (ta - tc);
-    const double W = t2 > t3 ? sqrt(t2 - t3) : 0.0;
-    const double iw = W > 0.0 ? 1.0 / W : 0.0;
-    const double dta = (o.dx2i - (o.dz2dx2 * (ta - tb) + o.dx2dy2 * (ta - tc)) * iw) / o.dsum;
-    const double dtb = (o.dz2i - (-o.dz2dx2 * (ta - tb) + o.dz2dy2 * (tb - tc)) * iw) / o.dsum;
-    const double dtc = (o.dy2i - (-o.dz2dy2 * (tb - tc) - o.dx2dy2 * (ta - tc)) * iw) / o.dsum;
+    const double t3 = o.dz2dx2 * dab * dab + o.dz2dy2 * dbc * dbc + o.dx2dy2 * dac * dac;
+    const double iw = t2 > t3 ? rsqrt(t2 - t3) : 0.0;  // 1 / W, W = sqrt(t2 - t3)
+    const double isum = o.rsum.hi;
+    const double dta = (o.dx2i - (o.dz2dx2 * dab + o.dx2dy2 * dac) * iw) * isum;
+    const double dtb = (o.dz2i - (o.dz2dy2 * dbc - o.dz2dx2 * dab) * iw) * isum;
+    const double dtc = (o.dy2i + (o.dz2dy2 * dbc + o.dx2dy2 * dac) * iw) * isum;
     // d(ta, tb, tc) / d(tv, te, tn, tev, ten, tnv, tnve)
-    w[3] = -0.5 * dta + dtb - 0.5 * dtc;        // tv
-    w[1] = dta - 0.5 * dtb - 0.5 * dtc;         // te
-    w[0] = -0.5 * dta - 0.5 * dtb + dtc;        // tn
-    w[5] = 0.5 * dta + 0.5 * dtb - dtc;         // tev
-    w[2] = 0.5 * dta - dtb + 0.5 * dtc;         // ten
-    w[4] = -dta + 0.5 * dtb + 0.5 * dtc;        // tnv
-    w[6] = dta + dtb + dtc;                     // tnve
+    const double hta = 0.5 * dta, htb = 0.5 * dtb, htc = 0.5 * dtc;
+    w[3] = dtb - hta - htc;  // tv
+    w[1] = dta - htb - htc;  // te
+    w[0] = dtc - hta - htb;  // tn
+    w[5] = hta + htb - dtc;  // tev
+    w[2] = hta + htc - dtb;  // ten
+    w[4] = htb + htc - dta;  // tnv
+    w[6] = dta + dtb + dtc;  // tnve
     ps = 9.0 * v * iw;
   }
-  if (ncell > 1) ps *= 0.5;
+  if (__popc(cells) > 1) ps *= 0.5;
 #undef T
-#undef C
 }
 
 // Slot of cell (ci, cj, ck) among the 8 cells around node (i, j, k)
@@ -336,6 +358,15 @@ __global__ void __launch_bounds__(kRevWarps * 32)
     const uint8_t* code_s = A.tcode + tbase;
     const double* old_s = A.told + tbase;
     const bool face_j = lj == PJW - 1, face_k = lk == PKW - 1;
+    // the cells around this column (rows along i are set per node)
+    const long long nxy_c = (long long)A.nx * A.ny;
+    CellFrame F;
+    F.x0 = (long long)imax(j - 1, 0) * A.ny;
+    F.x1 = (long long)imin(j, A.nx - 1) * A.ny;
+    F.xa = F.x1 != F.x0;
+    F.y0 = imax(k - 1, 0);
+    F.y1 = imin(k, A.ny - 1);
+    F.ya = F.y1 != F.y0;
 
     // What this lane sent across each slot 1, 2 and 3 steps ago.
     double h0 = nz0, h1 = nz0, h3 = nz0;                         // slots 0, 1, 3
@@ -402,19 +433,19 @@ __global__ void __launch_bounds__(kRevWarps * 32)
         } else {
           int az, ax, ay;
           decode(code, az, ax, ay);
+          F.z0 = (long long)imax(i - 1, 0) * nxy_c;
+          F.z1 = (long long)imin(i, A.nz - 1) * nxy_c;
+          F.za = F.z1 != F.z0;
           double w[kSlots], ps;
-          int cell[4], ncell;
-          linearize(az, ax, ay, i, j, k, n, tt_s, A.slow, A.nz, A.nx, A.ny, A.NX, A.NY, A.o, w,
-                    ps, cell, ncell);
+          unsigned cells;
+          linearize(az, ax, ay, i, j, k, n, tt_s, A.slow, F, A.NX, A.NY, A.o, w, ps, cells);
 #pragma unroll
           for (int q = 0; q < kSlots; ++q) {
             const int bz = (q + 1) >> 2, bx = ((q + 1) >> 1) & 1, by = (q + 1) & 1;
             if (uses_slot(az, ax, ay, bz, bx, by)) c[q] = lam * w[q];
           }
-          for (int q = 0; q < ncell; ++q) {
-            const int ci = cell[q] / (A.nx * A.ny), cj = (cell[q] / A.ny) % A.nx,
-                      ck = cell[q] % A.ny;
-            double* g = g8_s + n * 8 + cell_slot(i, j, k, ci, cj, ck);
+          for (unsigned m = cells; m; m &= m - 1) {
+            double* g = g8_s + n * 8 + (__ffs(m) - 1);
             *g = __ldcg(g) + lam * ps;
           }
           lam_s[n] = 0.0;

@@ -3,8 +3,9 @@
 // The kernels reproduce fteikpy's numba arithmetic operation by operation:
 // `x ** 2.0` is x*x, `x ** 0.5` is the correctly rounded sqrt, every other
 // operation is a single IEEE double operation in the reference's evaluation
-// order, and the library is compiled with --fmad=false so nothing is
-// contracted.  On GB300 the FP64 pipe is the bottleneck (about 1.2 TFLOP/s), so
+// order, and every file that computes the reference's results is compiled
+// with --fmad=false so nothing is contracted (only the adjoint's partials,
+// which have no bitwise counterpart, may contract).  On GB300 the FP64 pipe is the bottleneck (about 1.2 TFLOP/s), so
 // work that can leave it without changing a single result bit does:
 //
 //  * comparisons, min and max of doubles run on the integer pipe through an

@@ -7,12 +7,25 @@
 // and the 8 weights are computed once here and applied to the three
 // components, which gives the same numbers.
 //
+// On GB300 one warp's FP64 instruction occupies the FP64 pipe for 64 cycles
+// (a compare for about 105, a sqrt or a division for about 600), whatever the
+// number of active lanes, so a ray step is timed by its FP64 instruction
+// count.  Work that can leave the pipe without changing a result bit does:
+// comparisons of positions against axis values use integer order keys, the
+// cell guess is a float computation confirmed by exact comparisons, the
+// "distance to the source >= stepsize" test compares the squared distance
+// with the exact threshold of RN(sqrt(x)) >= stepsize (found on the host),
+// and on axes with one spacing the blend's division by the cell volume uses
+// the correctly rounded constant-divisor division of common.cuh.
+//
 // One intentional difference: when a honor_grid step lands exactly on the last
 // node of an axis, the reference reads one element past the end of that axis
 // (_ray3d.py:96-98, _ray2d.py:69-70); here the index is clamped to the last
 // node, as the reference itself does when it sets up the first cell
 // (_ray3d.py:46-48).
 #include <math_constants.h>
+
+#include <cmath>
 
 #include "common.cuh"
 #include "fteik_gb300.h"
@@ -57,71 +70,240 @@ struct Axes {
   int n[3];
 };
 
-// Gradient direction at p: the three (or two) interpolated components.
-template <int ND>
-__device__ __forceinline__ void grad_at(const Axes& ax, const double* g, const double* p,
-                                        double* out) {
-  if (ND == 3) {
-    if (!inside3(ax.a[0], ax.n[0], ax.a[1], ax.n[1], ax.a[2], ax.n[2], p[0], p[1], p[2])) {
-      out[0] = out[1] = out[2] = CUDART_NAN;
-      return;
-    }
-    const Cell3 c = locate3(ax.a[0], ax.n[0], ax.a[1], ax.n[1], ax.a[2], ax.n[2], p[0], p[1], p[2]);
-    double w[8];
-    weights3(c, p[0], p[1], p[2], w);
-#pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-      double q[8];
-      corners3(g + comp, 3, c, ax.n[1], ax.n[2], q);
-      out[comp] = blend3(c, q, w);
-    }
-  } else {
-    if (!inside2(ax.a[0], ax.n[0], ax.a[1], ax.n[1], p[0], p[1])) {
-      out[0] = out[1] = CUDART_NAN;
-      return;
-    }
-    const Cell2 c = locate2(ax.a[0], ax.n[0], ax.a[1], ax.n[1], p[0], p[1]);
-    double w[4];
-    weights2(c, p[0], p[1], w);
-#pragma unroll
-    for (int comp = 0; comp < 2; ++comp) {
-      double q[4];
-      corners2(g + comp, 2, c, ax.n[1], q);
-      double vq = q[0] * w[0];
-      vq += q[1] * w[1];
-      vq += q[2] * w[2];
-      vq += q[3] * w[3];
-      vq /= fabs((c.x2 - c.x1) * (c.y2 - c.y1));
-      out[comp] = vq;
-    }
-  }
+// Order key of a non-NaN double in which -0.0 and +0.0 are equal:
+// zkey(a) < zkey(b) <=> a < b.
+__device__ __forceinline__ long long zkey(double x) {
+  const long long b = __double_as_longlong(x);
+  const long long m = b & 0x7fffffffffffffffLL;
+  return b < 0 ? -m : m;
 }
 
-// Component `comp` of grad_at (the same lookup, weights and blend).
-template <int ND>
-__device__ __forceinline__ double grad_comp(const Axes& ax, const double* g, const double* p,
-                                            int comp) {
-  if (ND == 3) {
-    if (!inside3(ax.a[0], ax.n[0], ax.a[1], ax.n[1], ax.a[2], ax.n[2], p[0], p[1], p[2]))
-      return CUDART_NAN;
-    const Cell3 c = locate3(ax.a[0], ax.n[0], ax.a[1], ax.n[1], ax.a[2], ax.n[2], p[0], p[1], p[2]);
-    double w[8], q[8];
-    weights3(c, p[0], p[1], p[2], w);
-    corners3(g + comp, 3, c, ax.n[1], ax.n[2], q);
-    return blend3(c, q, w);
+// Per-axis constants of one launch, set up by every block in shared memory.
+struct RayAxis {
+  double lo, hi;       // first and last node
+  long long klo, khi;  // their order keys
+  float f0, fs;        // cell guess (float(v) - f0) * fs
+  int uniform;         // every cell (and the last-node extension) has x2 - x1 == d
+  double d;
+};
+
+// np.searchsorted(a, v, "right") - 1 for a finite v with lo <= v <= hi: the
+// float guess, confirmed (or moved by one) with exact comparisons, else a
+// bisection.
+__device__ __forceinline__ int ray_search(const double* __restrict__ a, int n,
+                                          const RayAxis& X, double v, long long kv) {
+  if (kv >= X.khi) return n - 1;
+  int g = (int)(((float)v - X.f0) * X.fs);
+  g = g < 0 ? 0 : (g > n - 2 ? n - 2 : g);
+  const long long kg = zkey(__ldg(a + g));
+  int lo, hi;  // invariant: a[lo] <= v < a[hi]
+  if (kg <= kv) {
+    const long long kg1 = zkey(__ldg(a + g + 1));
+    if (kv < kg1) return g;
+    if (g + 2 > n - 1 || kv < zkey(__ldg(a + g + 2))) return g + 1;  // a[n-1] > v here
+    lo = g + 2;
+    hi = n - 1;
   } else {
-    if (!inside2(ax.a[0], ax.n[0], ax.a[1], ax.n[1], p[0], p[1])) return CUDART_NAN;
-    const Cell2 c = locate2(ax.a[0], ax.n[0], ax.a[1], ax.n[1], p[0], p[1]);
+    if (g > 0 && zkey(__ldg(a + g - 1)) <= kv) return g - 1;
+    lo = 0;
+    hi = g;
+  }
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (zkey(__ldg(a + mid)) <= kv)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Per-launch state every block sets up in shared memory.
+struct RayShared {
+  RayAxis X[3];
+  Recip vol;      // 1 / cell volume when every axis has one spacing
+  int uni;        // 1: divide blends with `vol`
+  double vol_c;   // the cell volume
+};
+
+// RN(x / cell volume) as _interp3d computes it: the constant-divisor
+// division where it is exact (one spacing per axis, x normal and far from
+// overflow and underflow), else IEEE division by the volume of cell c.
+__device__ __forceinline__ double per_volume(double x, double vol_c, const Recip& R, bool uni) {
+  const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  if (uni && e >= 300 && e <= 1700) return div_by(x, R);
+  return x / vol_c;
+}
+
+// Component `comp` of the gradient at p (the reference interpolates each
+// component with _interp3d / _interp2d, _ray3d.py:60-62): NaN outside.
+template <int ND>
+__device__ __forceinline__ double grad_comp(const Axes& ax, const RayShared& S, const double* g,
+                                            const double* p, const long long* kp, int comp) {
+  bool inside = true;
+#pragma unroll
+  for (int q = 0; q < ND; ++q) inside = inside && S.X[q].klo <= kp[q] && kp[q] <= S.X[q].khi;
+  if (!inside) return CUDART_NAN;
+  if (ND == 3) {
+    Cell3 c;
+    c.i1 = ray_search(ax.a[0], ax.n[0], S.X[0], p[0], kp[0]);
+    c.j1 = ray_search(ax.a[1], ax.n[1], S.X[1], p[1], kp[1]);
+    c.k1 = ray_search(ax.a[2], ax.n[2], S.X[2], p[2], kp[2]);
+    const int nx = ax.n[0], ny = ax.n[1], nz = ax.n[2];
+    c.ei = c.i1 == nx - 1;
+    c.ej = c.j1 == ny - 1;
+    c.ek = c.k1 == nz - 1;
+    c.x1 = __ldg(ax.a[0] + c.i1);
+    c.y1 = __ldg(ax.a[1] + c.j1);
+    c.z1 = __ldg(ax.a[2] + c.k1);
+    c.x2 = c.ei ? 2.0 * c.x1 - __ldg(ax.a[0] + nx - 2) : __ldg(ax.a[0] + c.i1 + 1);
+    c.y2 = c.ej ? 2.0 * c.y1 - __ldg(ax.a[1] + ny - 2) : __ldg(ax.a[1] + c.j1 + 1);
+    c.z2 = c.ek ? 2.0 * c.z1 - __ldg(ax.a[2] + nz - 2) : __ldg(ax.a[2] + c.k1 + 1);
+    double w[8], q[8];
+    corners3(g + comp, 3, c, ny, nz, q);
+    weights3(c, p[0], p[1], p[2], w);
+    double vq = q[0] * w[0];
+#pragma unroll
+    for (int t = 1; t < 8; ++t) vq += q[t] * w[t];
+    const double vol = S.uni ? S.vol_c : fabs((c.x2 - c.x1) * (c.y2 - c.y1) * (c.z2 - c.z1));
+    return per_volume(vq, vol, S.vol, S.uni != 0);
+  } else {
+    Cell2 c;
+    c.i1 = ray_search(ax.a[0], ax.n[0], S.X[0], p[0], kp[0]);
+    c.j1 = ray_search(ax.a[1], ax.n[1], S.X[1], p[1], kp[1]);
+    const int nx = ax.n[0], ny = ax.n[1];
+    c.ei = c.i1 == nx - 1;
+    c.ej = c.j1 == ny - 1;
+    c.x1 = __ldg(ax.a[0] + c.i1);
+    c.y1 = __ldg(ax.a[1] + c.j1);
+    c.x2 = c.ei ? 2.0 * c.x1 - __ldg(ax.a[0] + nx - 2) : __ldg(ax.a[0] + c.i1 + 1);
+    c.y2 = c.ej ? 2.0 * c.y1 - __ldg(ax.a[1] + ny - 2) : __ldg(ax.a[1] + c.j1 + 1);
     double w[4], q[4];
+    corners2(g + comp, 2, c, ny, q);
     weights2(c, p[0], p[1], w);
-    corners2(g + comp, 2, c, ax.n[1], q);
     double vq = q[0] * w[0];
     vq += q[1] * w[1];
     vq += q[2] * w[2];
     vq += q[3] * w[3];
-    vq /= fabs((c.x2 - c.x1) * (c.y2 - c.y1));
-    return vq;
+    const double vol = S.uni ? S.vol_c : fabs((c.x2 - c.x1) * (c.y2 - c.y1));
+    return per_volume(vq, vol, S.vol, S.uni != 0);
   }
+}
+
+// All components at p (one lane per ray): the lookup and weights once.
+template <int ND>
+__device__ __forceinline__ void grad_at(const Axes& ax, const RayShared& S, const double* g,
+                                        const double* p, const long long* kp, double* out) {
+  bool inside = true;
+#pragma unroll
+  for (int q = 0; q < ND; ++q) inside = inside && S.X[q].klo <= kp[q] && kp[q] <= S.X[q].khi;
+  if (!inside) {
+#pragma unroll
+    for (int q = 0; q < ND; ++q) out[q] = CUDART_NAN;
+    return;
+  }
+  if (ND == 3) {
+    Cell3 c;
+    c.i1 = ray_search(ax.a[0], ax.n[0], S.X[0], p[0], kp[0]);
+    c.j1 = ray_search(ax.a[1], ax.n[1], S.X[1], p[1], kp[1]);
+    c.k1 = ray_search(ax.a[2], ax.n[2], S.X[2], p[2], kp[2]);
+    const int nx = ax.n[0], ny = ax.n[1], nz = ax.n[2];
+    c.ei = c.i1 == nx - 1;
+    c.ej = c.j1 == ny - 1;
+    c.ek = c.k1 == nz - 1;
+    c.x1 = __ldg(ax.a[0] + c.i1);
+    c.y1 = __ldg(ax.a[1] + c.j1);
+    c.z1 = __ldg(ax.a[2] + c.k1);
+    c.x2 = c.ei ? 2.0 * c.x1 - __ldg(ax.a[0] + nx - 2) : __ldg(ax.a[0] + c.i1 + 1);
+    c.y2 = c.ej ? 2.0 * c.y1 - __ldg(ax.a[1] + ny - 2) : __ldg(ax.a[1] + c.j1 + 1);
+    c.z2 = c.ek ? 2.0 * c.z1 - __ldg(ax.a[2] + nz - 2) : __ldg(ax.a[2] + c.k1 + 1);
+    double w[8];
+    weights3(c, p[0], p[1], p[2], w);
+    const double vol = S.uni ? S.vol_c : fabs((c.x2 - c.x1) * (c.y2 - c.y1) * (c.z2 - c.z1));
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+      double q[8];
+      corners3(g + comp, 3, c, ny, nz, q);
+      double vq = q[0] * w[0];
+#pragma unroll
+      for (int t = 1; t < 8; ++t) vq += q[t] * w[t];
+      out[comp] = per_volume(vq, vol, S.vol, S.uni != 0);
+    }
+  } else {
+    Cell2 c;
+    c.i1 = ray_search(ax.a[0], ax.n[0], S.X[0], p[0], kp[0]);
+    c.j1 = ray_search(ax.a[1], ax.n[1], S.X[1], p[1], kp[1]);
+    const int nx = ax.n[0], ny = ax.n[1];
+    c.ei = c.i1 == nx - 1;
+    c.ej = c.j1 == ny - 1;
+    c.x1 = __ldg(ax.a[0] + c.i1);
+    c.y1 = __ldg(ax.a[1] + c.j1);
+    c.x2 = c.ei ? 2.0 * c.x1 - __ldg(ax.a[0] + nx - 2) : __ldg(ax.a[0] + c.i1 + 1);
+    c.y2 = c.ej ? 2.0 * c.y1 - __ldg(ax.a[1] + ny - 2) : __ldg(ax.a[1] + c.j1 + 1);
+    double w[4];
+    weights2(c, p[0], p[1], w);
+    const double vol = S.uni ? S.vol_c : fabs((c.x2 - c.x1) * (c.y2 - c.y1));
+#pragma unroll
+    for (int comp = 0; comp < 2; ++comp) {
+      double q[4];
+      corners2(g + comp, 2, c, ny, q);
+      double vq = q[0] * w[0];
+      vq += q[1] * w[1];
+      vq += q[2] * w[2];
+      vq += q[3] * w[3];
+      out[comp] = per_volume(vq, vol, S.vol, S.uni != 0);
+    }
+  }
+}
+
+// The block's shared set-up: axis ends and keys, the float guess, and
+// whether every axis has a single spacing d (a[i+1] - a[i] == d for every
+// cell and for the last-node extension 2*a[n-1] - a[n-2]), which makes every
+// cell volume the same double.
+template <int ND>
+__device__ __forceinline__ void ray_setup(const Axes& ax, RayShared& S) {
+  if (threadIdx.x < ND) {
+    const int q = threadIdx.x;
+    const double* a = ax.a[q];
+    const int n = ax.n[q];
+    RayAxis& X = S.X[q];
+    X.lo = __ldg(a);
+    X.hi = __ldg(a + n - 1);
+    X.klo = zkey(X.lo);
+    X.khi = zkey(X.hi);
+    X.f0 = (float)X.lo;
+    const float span = (float)X.hi - X.f0;
+    X.fs = span > 0.0f ? (float)(n - 1) / span : 0.0f;
+    X.d = __ldg(a + 1) - __ldg(a);
+    X.uniform = deq((2.0 * X.hi - __ldg(a + n - 2)) - X.hi, X.d) ? 1 : 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < ND; ++q) {
+    const double* a = ax.a[q];
+    bool ok = true;
+    for (int i = threadIdx.x; i < ax.n[q] - 1; i += blockDim.x)
+      ok = ok && deq(__ldg(a + i + 1) - __ldg(a + i), S.X[q].d);
+    if (!ok) S.X[q].uniform = 0;  // benign race: every writer stores 0
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool uni = true;
+    double vol = 1.0;
+#pragma unroll
+    for (int q = 0; q < ND; ++q) {
+      uni = uni && S.X[q].uniform;
+      vol = vol * S.X[q].d;
+    }
+    vol = fabs(vol);
+    // the constant-divisor division wants a normal divisor of moderate size
+    const int e = (int)((__double_as_longlong(vol) >> 52) & 0x7ff);
+    uni = uni && e >= 823 && e <= 1223;
+    S.uni = uni ? 1 : 0;
+    S.vol_c = vol;
+    S.vol = make_recip(uni ? vol : 1.0);
+  }
+  __syncthreads();
 }
 
 // _ray3d / _ray2d, _ray3d.py:9-120 and _ray2d.py:9-91.
@@ -129,11 +311,15 @@ __device__ __forceinline__ double grad_comp(const Axes& ax, const double* g, con
 // one gradient component and the group shares them, so a few rays (one
 // source's receivers) take fewer dependent FP64 instructions per step; the
 // other work is done identically by every lane and lane 0 writes.
+// `dist_min` is the least double x with RN(sqrt(x)) >= stepsize, so the
+// reference's `dist(src, p) >= stepsize` is `squared distance >= dist_min`.
 template <int ND, int L>
 __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, const int* gidx,
                            const double* ends, int nrays, const double* sources,
-                           double stepsize, int max_step, int honor_grid, double* rays,
-                           int* counts, int* status) {
+                           double stepsize, double dist_min, int max_step, int honor_grid,
+                           double* rays, int* counts, int* status) {
+  __shared__ RayShared S;
+  ray_setup<ND>(ax, S);
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int r = (int)(tid / L);
   const int sub = (int)(tid % L);
@@ -142,7 +328,9 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
   if (r >= nrays) return;
   const int gi = gidx ? gidx[r] : 0;
   const double* g = ttgrad + (long long)gi * gstride;
+  const long long kmin = __double_as_longlong(dist_min);
   double src[ND], pcur[ND], delta[ND], lower[ND], upper[ND];
+  long long kp[ND];
   int isrc[ND];
 #pragma unroll
   for (int q = 0; q < ND; ++q) {
@@ -152,10 +340,11 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
   if (writer) counts[r] = 0;
 #pragma unroll
   for (int q = 0; q < ND; ++q) {
-    if (!(__ldg(ax.a[q]) <= pcur[q] && pcur[q] <= __ldg(ax.a[q] + ax.n[q] - 1))) {
+    if (!(S.X[q].lo <= pcur[q] && pcur[q] <= S.X[q].hi)) {
       if (writer) status[r] = kEndPointOutOfBound;
       return;
     }
+    kp[q] = zkey(pcur[q]);
   }
   if (honor_grid) {
 #pragma unroll
@@ -184,25 +373,33 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
       if (writer) status[r] = kMaxStepReached;
       return;
     }
-    const double dd = ND == 3 ? dist3(src[0], src[1], src[2], pcur[0], pcur[1], pcur[2])
-                              : dist2(src[0], src[1], pcur[0], pcur[1]);
-    if (!(dd >= stepsize)) break;
+    // dist(src, pcur) >= stepsize: the squared distance is a sum of squares,
+    // so as a bit pattern it orders like its value; NaN (a NaN position)
+    // fails the reference's test
+    double dsq;
+    if (ND == 3) {
+      const double a = src[0] - pcur[0], b = src[1] - pcur[1], c = src[2] - pcur[2];
+      dsq = a * a + b * b + c * c;
+    } else {
+      const double a = src[0] - pcur[0], b = src[1] - pcur[1];
+      dsq = a * a + b * b;
+    }
+    const long long db = __double_as_longlong(dsq);
+    if (db < kmin || db > 0x7ff0000000000000LL) break;
     double gv[ND];
     if (L == 1) {
-      grad_at<ND>(ax, g, pcur, gv);
+      grad_at<ND>(ax, S, g, pcur, kp, gv);
     } else {
-      const double mine = sub < ND ? grad_comp<ND>(ax, g, pcur, sub) : 0.0;
+      const double mine = sub < ND ? grad_comp<ND>(ax, S, g, pcur, kp, sub) : 0.0;
 #pragma unroll
       for (int q = 0; q < ND; ++q) gv[q] = __shfl_sync(gmask, mine, q, L);
     }
     double gsq = gv[0] * gv[0] + gv[1] * gv[1];
     if (ND == 3) gsq = gsq + gv[ND - 1] * gv[ND - 1];
-    const double gn = sqrt(gsq);
-    double gni;
-    if (gn > 0.0)
-      gni = 1.0 / gn;
-    else
-      break;
+    // gn = sqrt(gsq) > 0 unless gsq is +0 or NaN (a sum of squares)
+    const long long gb = __double_as_longlong(gsq);
+    if (gb == 0 || gb > 0x7ff0000000000000LL) break;
+    const double gni = 1.0 / sqrt(gsq);
 #pragma unroll
     for (int q = 0; q < ND; ++q) delta[q] = stepsize * gv[q] * gni;
     if (honor_grid) {
@@ -210,7 +407,7 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
 #pragma unroll
       for (int q = 0; q < ND; ++q) {
         double v = pcur[q] - fac * delta[q];
-        const double lo = __ldg(ax.a[q]), hi = __ldg(ax.a[q] + ax.n[q] - 1);
+        const double lo = S.X[q].lo, hi = S.X[q].hi;
         v = lo > v ? lo : v;  // max(pcur, axis[0])
         v = hi < v ? hi : v;  // min(., axis[-1])
         pcur[q] = v;
@@ -240,14 +437,26 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
         count += 1;
         if (hit) break;
       }
+#pragma unroll
+      for (int q = 0; q < ND; ++q) kp[q] = zkey(pcur[q]);
     } else {
 #pragma unroll
       for (int q = 0; q < ND; ++q) {
+        // max(axis[0], min(axis[-1], pcur - delta)) with the comparisons on
+        // keys; a NaN compares false with both ends and stays
         double v = pcur[q] - delta[q];
-        const double lo = __ldg(ax.a[q]), hi = __ldg(ax.a[q] + ax.n[q] - 1);
-        v = lo > v ? lo : v;
-        v = hi < v ? hi : v;
+        long long kv = zkey(v);
+        const bool nan = (kv < 0 ? -kv : kv) > 0x7ff0000000000000LL;
+        if (!nan && S.X[q].klo > kv) {
+          v = S.X[q].lo;
+          kv = S.X[q].klo;
+        }
+        if (!nan && S.X[q].khi < kv) {
+          v = S.X[q].hi;
+          kv = S.X[q].khi;
+        }
         pcur[q] = v;
+        kp[q] = kv;
         if (writer) ray[count * ND + q] = v;
       }
       count += 1;
@@ -285,6 +494,23 @@ __global__ void ray_pack_kernel(const double* rays, int nrays, int max_step, con
 
 using namespace fteik;
 
+// The least double x >= 0 with RN(sqrt(x)) >= s (s > 0): RN(sqrt(.)) is
+// monotone, so sqrt(x) >= s exactly when x >= this threshold.  The host's
+// sqrt is the correctly rounded IEEE square root, as the device's is.
+static double sqrt_threshold(double s) {
+  double x = s * s;
+  if (!(std::sqrt(x) >= s)) {
+    while (!(std::sqrt(x) >= s)) x = std::nextafter(x, HUGE_VAL);
+  } else {
+    for (;;) {
+      const double y = std::nextafter(x, 0.0);
+      if (!(y >= 0.0) || y == x || !(std::sqrt(y) >= s)) break;
+      x = y;
+    }
+  }
+  return x;
+}
+
 template <int ND>
 static int launch_rays(const double* const* axes, const int* n, const double* ttgrad,
                        long long grad_stride, const int* grid_index, const double* ends,
@@ -298,17 +524,18 @@ static int launch_rays(const double* const* axes, const int* n, const double* tt
     if (q < ND && n[q] < 2) return kInvalidArgument;
   }
   if (nrays == 0) return kOk;
+  const double dist_min = sqrt_threshold(stepsize);
   // Four lanes per ray while every ray's group fits on the GPU at once (one
   // source's receivers); one lane per ray for large batches, which are bound
   // by throughput rather than by the latency of a step.
   if ((long long)nrays * 4 <= 64LL * 1024) {
     const long long threads = (long long)nrays * 4;
     ray_kernel<ND, 4><<<(unsigned)((threads + 63) / 64), 64, 0, (cudaStream_t)stream>>>(
-        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, max_step,
+        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min, max_step,
         honor_grid, rays, counts, status);
   } else {
     ray_kernel<ND, 1><<<(nrays + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
-        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, max_step,
+        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min, max_step,
         honor_grid, rays, counts, status);
   }
   FTEIK_CHECK(cudaGetLastError());

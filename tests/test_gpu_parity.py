@@ -362,3 +362,56 @@ def test_rays_with_one_and_four_lanes_per_ray_agree():
     ref = O.raytrace(O.axes(tt.shape, d, np.zeros(3)), tg_o, ends[sample], src, 10.0, max_step,
                      False)
     assert all(np.array_equal(many[i], r) for i, r in zip(sample, ref))
+
+
+@pytest.mark.parametrize(
+    "nd,d,og,stepsize",
+    [
+        # spacings that are not exact in binary: x2 - x1 differs from cell to
+        # cell in the last bits, so the blends divide by each cell's volume
+        (3, (0.3, 0.7, 0.5), (0.3, -1.1, 0.7), None),
+        (3, (0.7, 0.3, 0.9), (0.1, 0.3, -0.7), None),
+        # one exact spacing per axis (the constant-volume division), a step
+        # that is not a multiple of the spacing
+        (3, (10.0, 12.0, 8.0), (3.0, -5.0, 7.0), 3.3),
+        (2, (0.3, 0.7), (0.3, 0.7), None),
+        (2, (5.0, 7.0), (-1.0, 2.0), None),
+    ],
+)
+def test_rays_bitwise_vs_oracle_on_exact_and_inexact_axes(nd, d, og, stepsize):
+    """Rays (no honor_grid) against the oracle bit for bit, on axes where every
+    cell has the same volume and on axes where the volumes differ by
+    rounding."""
+    rng = np.random.default_rng(17)
+    shape = (14, 17, 19)[:nd]
+    og = np.array(og)
+    v = 1500.0 + 40.0 * np.arange(shape[0]).reshape((-1,) + (1,) * (nd - 1)) * np.ones(shape)
+    v *= 1.0 + 0.05 * rng.uniform(-1.0, 1.0, shape)
+    ext = np.array(d) * np.array(shape)
+    src = og + np.concatenate([[0.0], rng.uniform(0.2, 0.8, nd - 1) * ext[1:]])
+    cls = fp.Eikonal3D if nd == 3 else fp.Eikonal2D
+    tt = cls(v, d, og).solve(src, nsweep=2, return_gradient=True)
+    tg = tt._gradient.cpu().numpy()
+    ax = model_axes(tt.shape, d, og)
+    hi = og + np.array(d) * (np.array(tt.shape) - 1)
+    rec = np.column_stack(
+        [np.full(120, og[0])] + [rng.uniform(og[q], hi[q], 120) for q in range(1, nd)]
+    )
+    rec[:5, 0] = hi[0]  # the far edge of the first axis: the last-node extension
+    step = min(d) if stepsize is None else stepsize
+    ms = default_max_step(tt.shape, d, step)
+    # rays the reference cannot finish (max_step) must fail here as well
+    fails = []
+    for i in range(len(rec)):
+        try:
+            O.raytrace(ax, tg, rec[i : i + 1], src, step, ms, False)
+        except RuntimeError:
+            fails.append(i)
+    for i in fails:
+        with pytest.raises(RuntimeError, match="maximum number of steps reached"):
+            tt.raytrace(rec[i], stepsize=step)
+    keep = np.setdiff1d(np.arange(len(rec)), fails)
+    got = tt.raytrace(rec[keep], stepsize=step)
+    ref = O.raytrace(ax, tg, rec[keep], src, step, ms, False)
+    assert [len(r) for r in got] == [len(r) for r in ref]
+    assert bitwise(np.concatenate(got), np.concatenate(ref))

@@ -85,3 +85,31 @@ REF_GRAD_2D_SRC35 = (-0.70710678, -0.70710678)  # at (0, 0), source (3.5, 3.5)
 # default nsweep=2; traveltime sums and honor_grid ray lengths from (0, 0[, 0]).
 REF_MESHIO_2D = dict(shape=(8, 10), source=(4.0, 5.0), tt_sum=378.23469225, ray_len=9)
 REF_MESHIO_3D = dict(shape=(8, 10, 12), source=(4.0, 5.0, 6.0), tt_sum=6909.90160991, ray_len=14)
+
+
+# A stand-in for the meshio module (not installed here): Mesh keeps what the
+# export passes and turns the (type, connectivity) list into blocks with
+# .type and .data, as meshio.Mesh does.
+class _CellBlock:
+    def __init__(self, cell_type, data):
+        self.type = cell_type
+        self.data = np.asarray(data)
+
+    def __len__(self):
+        return len(self.data)
+
+
+class _Mesh:
+    def __init__(self, points, cells, point_data=None, cell_data=None):
+        self.points = np.asarray(points)
+        self.cells = [_CellBlock(t, d) for t, d in cells]
+        self.point_data = dict(point_data or {})
+        self.cell_data = dict(cell_data or {})
+
+
+def stand_in_meshio():
+    import types
+
+    mod = types.ModuleType("meshio")
+    mod.Mesh = _Mesh
+    return mod

@@ -32,6 +32,7 @@ from helpers import (
     default_max_step,
     max_rel,
     model_axes,
+    stand_in_meshio,
 )
 from oracle import oracle as O
 
@@ -119,8 +120,14 @@ def test_known_answer_call_gradient_raytrace_2d():
     assert np.allclose([tt.gradient[c]([0.0, 0.0]) for c in range(2)], REF_GRAD_2D_SRC35, atol=1e-8)
 
 
-@pytest.mark.parametrize("case", [REF_MESHIO_2D, REF_MESHIO_3D])
-def test_known_answer_meshio_sums(case):
+@pytest.mark.parametrize("case,ray_sum", [(REF_MESHIO_2D, 64.0), (REF_MESHIO_3D, 169.0)])
+def test_known_answer_meshio(case, ray_sum, monkeypatch):
+    """The reference's meshio test (tests/test_meshio.py) on this library's
+    solve and rays, through grid_to_meshio / ray_to_meshio with a stand-in
+    for the meshio module."""
+    import sys
+
+    monkeypatch.setitem(sys.modules, "meshio", stand_in_meshio())
     nd = len(case["shape"])
     cls = fp.Eikonal3D if nd == 3 else fp.Eikonal2D
     eik = cls(np.ones(case["shape"]), (1.0,) * nd)
@@ -128,6 +135,19 @@ def test_known_answer_meshio_sums(case):
     assert np.allclose(tt.grid.sum(), case["tt_sum"], atol=1e-8)
     ray = tt.raytrace(np.zeros(nd), honor_grid=True)
     assert len(ray) == case["ray_len"]
+    mesh, mesh_ray = fp.grid_to_meshio(eik, tt), fp.ray_to_meshio(ray)
+    npts = int(np.prod(np.array(case["shape"]) + 1))
+    assert len(mesh.points) == npts
+    assert sum(len(cell) for cell in mesh.cells) == int(np.prod(case["shape"]))
+    assert mesh.point_data["Traveltime"][npts // 2] == 0.0
+    assert np.allclose(mesh.point_data["Traveltime"].sum(), case["tt_sum"])
+    for grad in mesh.point_data["Gradient"].T:
+        assert grad[npts // 2] == 0.0
+        assert np.allclose(grad.sum(), 0.0)
+    assert mesh.cell_data["Velocity"][0].sum() == int(np.prod(case["shape"]))
+    assert len(mesh_ray.points) == len(ray)
+    assert len(mesh_ray.cells[0].data) == len(ray) - 1
+    assert mesh_ray.cells[0].data.sum() == ray_sum
 
 
 # ------------------------------------------------------------- golden fixtures

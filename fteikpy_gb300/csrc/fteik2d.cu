@@ -88,6 +88,31 @@ __device__ double delta2(double t1, double tauv, double taue, double tauev, doub
   return dpoly >= 0.0 ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
 }
 
+// Comparisons of the node update.  K = false: IEEE comparisons, which keep
+// Python's NaN semantics (every comparison with NaN is false).  K = true:
+// integer order keys (common.cuh), exact when no value is NaN or -0.0.  The
+// sweeps produce neither from values that are neither (every radicand of the
+// operators is positive by a wide margin under its guard, and every
+// traveltime is a sum of non-negative terms), so the keys serve every source
+// whose first propagation left only finite values in the grid; an FP64
+// comparison costs more than an FP64 add on GB300, and this chain is one
+// thread long.
+__device__ __forceinline__ bool is_finite(double x) {
+  return (__double_as_longlong(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
+template <bool K>
+__device__ __forceinline__ bool lt2(double a, double b) {
+  return K ? dlt(a, b) : a < b;
+}
+template <bool K>
+__device__ __forceinline__ bool le2(double a, double b) {
+  return K ? dle(a, b) : a <= b;
+}
+template <bool K>
+__device__ __forceinline__ bool eq2(double a, double b) {
+  return K ? deq(a, b) : a == b;
+}
+
 // The inputs of one node update that do not depend on the previous node of
 // the pass: the previous column's te and tev, the node's own old value t0, and
 // the five slowness cells of the operators.
@@ -114,13 +139,9 @@ __device__ __forceinline__ In2 load_in2(const double* tt, const double* slow, in
 }
 
 // One node update, _fteik2d.py:70-187, from tv (the previous node of the
-// pass) and the other inputs.  Comparisons are IEEE comparisons here (not
-// integer keys): after a source on the model's far boundary the reference's
-// first propagation can leave NaN in tt, and Python's comparison and min
-// semantics on NaN must be kept (NaN-aware integer comparisons measured
-// slower on this one-thread chain).  Returns the node's value after the
-// update.
-template <bool GRAD>
+// pass) and the other inputs, with the comparisons of policy K (above).
+// Returns the node's value after the update.
+template <bool GRAD, bool K>
 __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const Ops2& o,
                                                 const Source2& sp, int i, int j, int sgntz,
                                                 int sgntx, int NX, double tv, const In2& q) {
@@ -130,29 +151,31 @@ __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const 
   const double t1d1 = tv + o.dz * vref;
   vref = pmin(q.sx0, q.sx1);
   const double t1d2 = te + o.dx * vref;
-  const double t1d = t1d2 < t1d1 ? t1d2 : t1d1;
+  const double t1d = lt2<K>(t1d2, t1d1) ? t1d2 : t1d1;
 
   double t2d = kBig;
   vref = q.s2;
   const int di = i - sp.zsi, dj = j - sp.xsi;
   if (di > kEpsin || di < -kEpsin || dj > kEpsin || dj < -kEpsin) {
     // plane-wave operators, _fteik2d.py:121-142
-    if (tv <= te + o.dx * vref && te <= tv + o.dz * vref && te >= tev && tv >= tev) {
+    if (le2<K>(tv, te + o.dx * vref) && le2<K>(te, tv + o.dz * vref) && le2<K>(tev, te) &&
+        le2<K>(tev, tv)) {
       const double ta = tev + te - tv;
       const double tb = tev - te + tv;
       const double d = ta - tb;
       t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(times4(vref * vref) * o.s2 - o.p2 * (d * d)),
                    o.r2);
-    } else if (te - tev <= div_by(o.dzz * vref, o.rhyp) && te - tev > 0.0) {
+    } else if (le2<K>(te - tev, div_by(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, te - tev)) {
       const double r = div_by(te - tev, o.rdz);
       t2d = te + o.dx * sqrt(vref * vref - r * r);
-    } else if (tv - tev <= div_by(o.dxx * vref, o.rhyp) && tv - tev > 0.0) {
+    } else if (le2<K>(tv - tev, div_by(o.dxx * vref, o.rhyp)) && lt2<K>(0.0, tv - tev)) {
       const double r = div_by(tv - tev, o.rdx);
       t2d = tv + o.dz * sqrt(vref * vref - r * r);
     }
   } else {
     // spherical (factored) operator near the source, _fteik2d.py:144-171
-    if (tv < te + o.dx * vref && te < tv + o.dz * vref && te >= tev && tv >= tev) {
+    if (lt2<K>(tv, te + o.dx * vref) && lt2<K>(te, tv + o.dz * vref) && le2<K>(tev, te) &&
+        le2<K>(tev, tv)) {
       double tzc, txc;
       const double t0c = t_anad2(i, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero, tzc, txc);
       const double tauv = tv - t_ana2(i - sgntz, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
@@ -167,15 +190,15 @@ __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const 
   // min(t0, t1d, t2d) with Python's semantics: keep the earlier argument
   // unless a later one compares strictly smaller.
   double tnew = t0;
-  if (t1d < tnew) tnew = t1d;
-  if (t2d < tnew) tnew = t2d;
-  if (!(tnew == t0)) {
+  if (lt2<K>(t1d, tnew)) tnew = t1d;
+  if (lt2<K>(t2d, tnew)) tnew = t2d;
+  if (!eq2<K>(tnew, t0)) {
     tt[n] = tnew;
     if (GRAD) {
       int a, b;
-      if (tnew == t1d1) {
+      if (eq2<K>(tnew, t1d1)) {
         a = sgntz; b = 0;
-      } else if (tnew == t1d2) {
+      } else if (eq2<K>(tnew, t1d2)) {
         a = 0; b = sgntx;
       } else {
         a = sgntz; b = sgntx;
@@ -191,7 +214,7 @@ __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const 
 // input of the next node is read while the current one is computed (the
 // previous column is complete, and this column's old values were written by
 // earlier passes), so the pass runs at the latency of the arithmetic chain.
-template <bool GRAD>
+template <bool GRAD, bool K>
 __device__ __forceinline__ void column_pass2d(double* tt, uint8_t* rec, const double* slow,
                                               const Ops2& o, const Source2& sp, int j, int i0,
                                               int i1, int sgnvz, int sgnvx, int sgntz,
@@ -203,9 +226,26 @@ __device__ __forceinline__ void column_pass2d(double* tt, uint8_t* rec, const do
     const bool more = i != i1;
     In2 nxt;
     if (more) nxt = load_in2(tt, slow, i + step, j, sgnvz, sgnvx, sgntz, sgntx, NZ, NX);
-    tv = node_update2d<GRAD>(tt, rec, o, sp, i, j, sgntz, sgntx, NX, tv, cur);
+    tv = node_update2d<GRAD, K>(tt, rec, o, sp, i, j, sgntz, sgntx, NX, tv, cur);
     if (!more) break;
     cur = nxt;
+  }
+}
+
+// The nsweep interleaved sweeps, _fteik2d.py:190-287 and 619-621.
+template <bool GRAD, bool K>
+__device__ __noinline__ void sweeps2d(double* tt, uint8_t* rec, const double* slow,
+                                      const Ops2& o, const Source2& sp, int nsweep, int NZ,
+                                      int NX) {
+  for (int sw = 0; sw < nsweep; ++sw) {
+    for (int j = 1; j < NX; ++j) {
+      column_pass2d<GRAD, K>(tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX);
+      column_pass2d<GRAD, K>(tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX);
+    }
+    for (int j = NX - 2; j >= 0; --j) {
+      column_pass2d<GRAD, K>(tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX);
+      column_pass2d<GRAD, K>(tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX);
+    }
   }
 }
 
@@ -216,7 +256,8 @@ template <bool GRAD>
 __global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const double* src,
                                                      int nsrc, int nz, int nx, int nsweep,
                                                      Ops2 o, double* tt_all, uint8_t* rec_all,
-                                                     Source2* params, double* vzero_out) {
+                                                     Source2* params, double* vzero_out,
+                                                     bool keys) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsrc) return;
   const int NZ = nz + 1, NX = nx + 1;
@@ -391,16 +432,18 @@ __global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const d
   params[s] = sp;
   vzero_out[s] = vzero;
 
-  for (int sw = 0; sw < nsweep; ++sw) {
-    for (int j = 1; j < NX; ++j) {
-      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX);
-      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX);
-    }
-    for (int j = NX - 2; j >= 0; --j) {
-      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX);
-      column_pass2d<GRAD>(tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX);
-    }
-  }
+  // The first propagation wrote rows zsi, zsi+1 and columns xsi, xsi+1 (the
+  // rest is Big).  If all of them are finite, no NaN or infinity arises in
+  // the sweeps and their comparisons can use integer keys.
+  bool finite = keys;
+  for (int jj = 0; jj < NX && finite; ++jj)
+    for (int r = zsi; r <= imin(zsi + 1, NZ - 1); ++r) finite = finite && is_finite(tt[(long long)r * NX + jj]);
+  for (int ii = 0; ii < NZ && finite; ++ii)
+    for (int c = xsi; c <= imin(xsi + 1, NX - 1); ++c) finite = finite && is_finite(tt[(long long)ii * NX + c]);
+  if (finite)
+    sweeps2d<GRAD, true>(tt, rec, slow, o, sp, nsweep, NZ, NX);
+  else
+    sweeps2d<GRAD, false>(tt, rec, slow, o, sp, nsweep, NZ, NX);
 }
 
 __global__ void fill2d_kernel(double* tt, uint8_t* rec, long long n) {
@@ -499,12 +542,13 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
                               cudaMemcpyHostToDevice, st));
   fill2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
   const int blocks = (nsrc + 31) / 32;
+  const bool keys = option_value(kOptSweep2dKeys) != 0;
   if (grad)
     solve2d_kernel<true><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt, rec,
-                                                 params, vzero);
+                                                 params, vzero, keys);
   else
     solve2d_kernel<false><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt,
-                                                  rec, params, vzero);
+                                                  rec, params, vzero, keys);
   FTEIK_CHECK(cudaGetLastError());
   if (grad) {
     grad2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, params, nsrc, nz + 1, nx + 1,

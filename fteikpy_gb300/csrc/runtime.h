@@ -36,7 +36,8 @@ enum Option : int {
   kOptKeepTest = 3,     // 3D unchanged-node test before the 2D/3D operators: 0 off
   kOptSweepTeam = 4,    // 3D team kernel (compacted operators): 1 on, 0 off
   kOptAdjointChunk = 5, // adjoint reverse sweeps: steps between progress publications
-  kOptCount = 6,
+  kOptSweep2dKeys = 6,  // 2D sweeps: 0 forces IEEE comparisons (else integer keys when exact)
+  kOptCount = 7,
 };
 long long option_value(int opt);
 

@@ -52,6 +52,9 @@ int fteik_kernel_timing(int on);
  * test that skips the 2D/3D operators of nodes that provably keep their value
  * (grids with equal spacings only). "adjoint_chunk": steps between progress
  * publications of the adjoint's reverse pass, a power of 2 up to 64.
+ * "sweep2d_keys": 0 makes the 2D sweeps compare with IEEE comparisons
+ * throughout (by default they use integer order keys for every source whose
+ * first propagation left only finite values, where the two agree).
  * Results are identical for every setting.
  * fteik_get_option reads a knob back. */
 int fteik_set_option(const char* name, long long value);

@@ -250,7 +250,22 @@ def test_solve3d_batched_equals_single(nsrc):
         ((13, 90), (10.0, 10.0), 3, 1, 3),
     ],
 )
-def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed):
+@pytest.mark.parametrize("keys", [-1, 0])
+def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys):
+    """Both comparison paths of the 2D sweeps (integer keys, the default for
+    sources whose first propagation is finite; IEEE comparisons, forced by
+    the "sweep2d_keys" option) against the oracle, bit for bit."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
+    try:
+        _solve2d_bitwise_case(shape, d, nsrc, nsweep, seed)
+    finally:
+        lib.fteik_set_option(b"sweep2d_keys", -1)
+
+
+def _solve2d_bitwise_case(shape, d, nsrc, nsweep, seed):
     rng = np.random.default_rng(seed)
     v = 1500.0 + 30.0 * np.arange(shape[0])[:, None] * np.ones(shape)
     v *= 1.0 + 0.1 * rng.uniform(-1.0, 1.0, shape)
@@ -435,3 +450,28 @@ def test_rays_bitwise_vs_oracle_on_exact_and_inexact_axes(nd, d, og, stepsize):
     ref = O.raytrace(ax, tg, rec[keep], src, step, ms, False)
     assert [len(r) for r in got] == [len(r) for r in ref]
     assert bitwise(np.concatenate(got), np.concatenate(ref))
+
+
+@pytest.mark.parametrize("keys", [-1, 0])
+def test_solve2d_sources_on_the_far_boundaries(keys):
+    """Sources on the bottom and right model edges (where the reference's first
+    propagation divides by zero, _fteik2d.py:444-445) next to interior ones,
+    in one launch: both comparison paths against the oracle, bit for bit."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(3)
+    shape, d = (40, 36), (10.0, 8.0)
+    v = 1500.0 + 30.0 * np.arange(shape[0])[:, None] * np.ones(shape)
+    v *= 1.0 + 0.1 * rng.uniform(-1.0, 1.0, shape)
+    zmax, xmax = shape[0] * d[0], shape[1] * d[1]
+    src = np.array([[zmax, 123.3], [55.5, 100.1], [zmax, xmax], [0.0, 77.7], [133.0, xmax],
+                    [zmax, 0.0], [211.1, 150.0]])
+    assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
+    try:
+        tts = fp.Eikonal2D(v, d).solve(src, nsweep=2, return_gradient=True)
+    finally:
+        lib.fteik_set_option(b"sweep2d_keys", -1)
+    tt_o, tg_o, vz_o = O.solve2d(1.0 / v, d, src, 2, True)
+    assert bitwise(np.stack([t.grid for t in tts]), tt_o)
+    assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)

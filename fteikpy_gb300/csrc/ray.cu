@@ -474,6 +474,168 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
   }
 }
 
+// The same rays without honor_grid, four lanes per ray, where lane q of the
+// group owns axis q (lanes past the last axis repeat it): its term of the
+// squared distance, its cell search and corner coordinates, its two weight
+// differences, its gradient component's blend, its coordinate's step and
+// clamp, and its coordinate of each ray point.  The group exchanges only
+// what the others need by shuffles, so a step issues each axis's integer
+// work once instead of once per axis on every lane.  Every value is the same
+// IEEE operation on the same operands as in ray_kernel, so the rays are the
+// same bits.
+template <int ND>
+__global__ void ray_axis_kernel(Axes ax, const double* ttgrad, long long gstride,
+                                const int* gidx, const double* ends, int nrays,
+                                const double* sources, double stepsize, double dist_min,
+                                int max_step, double* rays, int* counts, int* status) {
+  __shared__ RayShared S;
+  ray_setup<ND>(ax, S);
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int r = (int)(tid >> 2);
+  const int sub = (int)(tid & 3);
+  const int q = sub < ND ? sub : ND - 1;
+  const int g0 = (threadIdx.x & 31) & ~3;  // first lane of the group
+  const unsigned gmask = 0xfu << g0;
+  const unsigned all_axes = (1u << ND) - 1u;
+  if (r >= nrays) return;
+  const int gi = gidx ? gidx[r] : 0;
+  const double* g = ttgrad + (long long)gi * gstride;
+  // (selects, not an index into the parameter block, which would copy it to
+  // local memory)
+  const double* a = q == 0 ? ax.a[0] : (q == 1 ? ax.a[1] : ax.a[ND - 1]);
+  const int n = q == 0 ? ax.n[0] : (q == 1 ? ax.n[1] : ax.n[ND - 1]);
+  const RayAxis& X = S.X[q];
+  const double sq = sources[ND * gi + q];
+  double p = ends[ND * r + q];
+  const long long kmin = __double_as_longlong(dist_min);
+  if (sub == 0) counts[r] = 0;
+  if (((__ballot_sync(gmask, X.lo <= p && p <= X.hi) >> g0) & all_axes) != all_axes) {
+    if (sub == 0) status[r] = kEndPointOutOfBound;
+    return;
+  }
+  long long kp = zkey(p);
+  double* ray = rays + (long long)r * max_step * ND;
+  int count = 1;
+  if (sub < ND) ray[q] = p;
+  const long long max_iter = 64LL * max_step + 4096;
+  for (long long iter = 0;; ++iter) {
+    if (iter >= max_iter) {
+      if (sub == 0) status[r] = kMaxStepReached;
+      return;
+    }
+    // dist(src, pcur) >= stepsize on the squared distance (a*a + b*b) + c*c
+    const double dq = sq - p;
+    const double s2 = dq * dq;
+    double dsq = __shfl_sync(gmask, s2, g0) + __shfl_sync(gmask, s2, g0 + 1);
+    if (ND == 3) dsq = dsq + __shfl_sync(gmask, s2, g0 + 2);
+    const long long db = __double_as_longlong(dsq);
+    if (db < kmin || db > 0x7ff0000000000000LL) break;
+    // outside the grid the gradient is NaN and the reference's loop ends
+    if (((__ballot_sync(gmask, X.klo <= kp && kp <= X.khi) >> g0) & all_axes) != all_axes) break;
+    // this lane's axis: cell, corner coordinates, weight differences
+    const int c = ray_search(a, n, X, p, kp);
+    const bool e = c == n - 1;
+    const double x1 = __ldg(a + c);
+    const double x2 = e ? 2.0 * x1 - __ldg(a + n - 2) : __ldg(a + c + 1);
+    const double lo = x1 - p, hi = x2 - p, span = x2 - x1;
+    double L[ND], H[ND];
+    int ci[ND];
+    bool ce[ND];
+#pragma unroll
+    for (int t = 0; t < ND; ++t) {
+      L[t] = __shfl_sync(gmask, lo, g0 + t);
+      H[t] = __shfl_sync(gmask, hi, g0 + t);
+      const int packed = __shfl_sync(gmask, (c << 1) | (e ? 1 : 0), g0 + t);
+      ci[t] = packed >> 1;
+      ce[t] = (packed & 1) != 0;
+    }
+    double vol = S.vol_c;
+    if (!S.uni) {
+      vol = __shfl_sync(gmask, span, g0) * __shfl_sync(gmask, span, g0 + 1);
+      if (ND == 3) vol = vol * __shfl_sync(gmask, span, g0 + 2);
+      vol = fabs(vol);
+    }
+    double mine;
+    if (ND == 3) {
+      // weights3: |((x? - xq) * (y? - yq)) * (z? - zq)|, 111, 211, 121, 221, 112, ...
+      const double hh = H[0] * H[1], lh = L[0] * H[1], hl = H[0] * L[1], ll = L[0] * L[1];
+      double w[8];
+      w[0] = fabs(hh * H[ND - 1]);
+      w[1] = fabs(lh * H[ND - 1]);
+      w[2] = fabs(hl * H[ND - 1]);
+      w[3] = fabs(ll * H[ND - 1]);
+      w[4] = fabs(hh * L[ND - 1]);
+      w[5] = fabs(lh * L[ND - 1]);
+      w[6] = fabs(hl * L[ND - 1]);
+      w[7] = fabs(ll * L[ND - 1]);
+      Cell3 cc;
+      cc.i1 = ci[0];
+      cc.j1 = ci[1];
+      cc.k1 = ci[ND - 1];
+      cc.ei = ce[0];
+      cc.ej = ce[1];
+      cc.ek = ce[ND - 1];
+      double qv[8];
+      corners3(g + q, 3, cc, ax.n[1], ax.n[ND - 1], qv);
+      double vq = qv[0] * w[0];
+#pragma unroll
+      for (int t = 1; t < 8; ++t) vq += qv[t] * w[t];
+      mine = per_volume(vq, vol, S.vol, S.uni != 0);
+    } else {
+      double w[4];
+      w[0] = fabs(H[0] * H[1]);
+      w[1] = fabs(L[0] * H[1]);
+      w[2] = fabs(H[0] * L[1]);
+      w[3] = fabs(L[0] * L[1]);
+      Cell2 cc;
+      cc.i1 = ci[0];
+      cc.j1 = ci[1];
+      cc.ei = ce[0];
+      cc.ej = ce[1];
+      double qv[4];
+      corners2(g + q, 2, cc, ax.n[1], qv);
+      double vq = qv[0] * w[0];
+      vq += qv[1] * w[1];
+      vq += qv[2] * w[2];
+      vq += qv[3] * w[3];
+      mine = per_volume(vq, vol, S.vol, S.uni != 0);
+    }
+    double gv[ND];
+#pragma unroll
+    for (int t = 0; t < ND; ++t) gv[t] = __shfl_sync(gmask, mine, g0 + t);
+    double gsq = gv[0] * gv[0] + gv[1] * gv[1];
+    if (ND == 3) gsq = gsq + gv[ND - 1] * gv[ND - 1];
+    const long long gb = __double_as_longlong(gsq);
+    if (gb == 0 || gb > 0x7ff0000000000000LL) break;
+    const double gni = 1.0 / sqrt(gsq);
+    // this lane's coordinate: max(axis[0], min(axis[-1], p - stepsize * g * gni))
+    double v = p - stepsize * mine * gni;
+    long long kv = zkey(v);
+    const bool nan = (kv < 0 ? -kv : kv) > 0x7ff0000000000000LL;
+    if (!nan && X.klo > kv) {
+      v = X.lo;
+      kv = X.klo;
+    }
+    if (!nan && X.khi < kv) {
+      v = X.hi;
+      kv = X.khi;
+    }
+    p = v;
+    kp = kv;
+    if (sub < ND) ray[count * ND + q] = v;
+    count += 1;
+    if (count >= max_step) {
+      if (sub == 0) status[r] = kMaxStepReached;
+      return;
+    }
+  }
+  if (sub < ND) ray[count * ND + q] = sq;
+  if (sub == 0) {
+    counts[r] = count;
+    status[r] = kOk;
+  }
+}
+
 // Reverse each ray (source first, as ray3d returns ray[count::-1]) and pack
 // the rays back to back.
 template <int ND>
@@ -530,9 +692,15 @@ static int launch_rays(const double* const* axes, const int* n, const double* tt
   // by throughput rather than by the latency of a step.
   if ((long long)nrays * 4 <= 64LL * 1024) {
     const long long threads = (long long)nrays * 4;
-    ray_kernel<ND, 4><<<(unsigned)((threads + 63) / 64), 64, 0, (cudaStream_t)stream>>>(
-        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min, max_step,
-        honor_grid, rays, counts, status);
+    const unsigned blocks = (unsigned)((threads + 63) / 64);
+    if (!honor_grid)
+      ray_axis_kernel<ND><<<blocks, 64, 0, (cudaStream_t)stream>>>(
+          ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min,
+          max_step, rays, counts, status);
+    else
+      ray_kernel<ND, 4><<<blocks, 64, 0, (cudaStream_t)stream>>>(
+          ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min,
+          max_step, honor_grid, rays, counts, status);
   } else {
     ray_kernel<ND, 1><<<(nrays + 63) / 64, 64, 0, (cudaStream_t)stream>>>(
         ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min, max_step,

@@ -249,28 +249,25 @@ __device__ __noinline__ void sweeps2d(double* tt, uint8_t* rec, const double* sl
   }
 }
 
-// Source classification and first propagation, _fteik2d.py:296-617, then the
-// nsweep interleaved sweeps, _fteik2d.py:190-287 and 619-621.  One thread per
-// source.  tt is pre-filled with Big and rec with "no sign".
+// Source classification and first propagation, _fteik2d.py:296-617, for the
+// source at src[0..1] into tt (pre-filled with Big; rec with "no sign").
+// Returns the source's parameters for the sweeps.
 template <bool GRAD>
-__global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const double* src,
-                                                     int nsrc, int nz, int nx, int nsweep,
-                                                     Ops2 o, double* tt_all, uint8_t* rec_all,
-                                                     Source2* params, double* vzero_out,
-                                                     bool keys) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsrc) return;
+__device__ Source2 first_propagation2d(const double* slow, const double* src, int nz, int nx,
+                                       const Ops2& o, double* tt, uint8_t* rec) {
   const int NZ = nz + 1, NX = nx + 1;
-  const long long nodes = (long long)NZ * NX;
-  double* tt = tt_all + (long long)s * nodes;
-  uint8_t* rec = GRAD ? rec_all + (long long)s * nodes : nullptr;
+#define TT(a, b) tt[(long long)(a)*NX + (b)]
+#define SL(a, b) slow[(long long)(a)*nx + (b)]
+#define SGN(a, b, sz_, sx_) \
+  if (GRAD) rec[(long long)(a)*NX + (b)] = (uint8_t)(((sz_) + 1) * 3 + ((sx_) + 1))
+
   const double dz = o.dz, dx = o.dx;
 #define TT(a, b) tt[(long long)(a)*NX + (b)]
 #define SL(a, b) slow[(long long)(a)*nx + (b)]
 #define SGN(a, b, sz_, sx_) \
   if (GRAD) rec[(long long)(a)*NX + (b)] = (uint8_t)(((sz_) + 1) * 3 + ((sx_) + 1))
 
-  double zsa = src[2 * s] / dz, xsa = src[2 * s + 1] / dx;
+  double zsa = src[0] / dz, xsa = src[1] / dx;
   zsa = zsa >= nz ? zsa - kEps : zsa;
   xsa = xsa >= nx ? xsa - kEps : xsa;
   const int zsi = imin((int)zsa, nz - 1);
@@ -429,8 +426,28 @@ __global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const d
   sp.xsi = xsi;
   sp.iflag = iflag;
   sp.pad = 0;
+  return sp;
+}
+
+// One thread per source: the first propagation, then the nsweep interleaved
+// sweeps, _fteik2d.py:190-287 and 619-621.  tt is pre-filled with Big and rec
+// with "no sign".
+template <bool GRAD>
+__global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const double* src,
+                                                     int nsrc, int nz, int nx, int nsweep,
+                                                     Ops2 o, double* tt_all, uint8_t* rec_all,
+                                                     Source2* params, double* vzero_out,
+                                                     bool keys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsrc) return;
+  const int NZ = nz + 1, NX = nx + 1;
+  const long long nodes = (long long)NZ * NX;
+  double* tt = tt_all + (long long)s * nodes;
+  uint8_t* rec = GRAD ? rec_all + (long long)s * nodes : nullptr;
+  const Source2 sp = first_propagation2d<GRAD>(slow, src + 2 * s, nz, nx, o, tt, rec);
+  const int zsi = sp.zsi, xsi = sp.xsi;
   params[s] = sp;
-  vzero_out[s] = vzero;
+  vzero_out[s] = sp.vzero;
 
   // The first propagation wrote rows zsi, zsi+1 and columns xsi, xsi+1 (the
   // rest is Big).  If all of them are finite, no NaN or infinity arises in
@@ -444,6 +461,211 @@ __global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const d
     sweeps2d<GRAD, true>(tt, rec, slow, o, sp, nsweep, NZ, NX);
   else
     sweeps2d<GRAD, false>(tt, rec, slow, o, sp, nsweep, NZ, NX);
+}
+
+// ----------------------------------------------------- one warp per source --
+//
+// For a few sources the chain's length is the solve's time, and every FP64
+// instruction of it costs the full warp issue time whatever the number of
+// active lanes.  Once column j - sgntx is final, every quantity of column j's
+// updates that does not involve tv (the previous node of the pass) is known:
+// the 1D candidates' terms, the plane operator's guards and partial sums,
+// its radicand's constant term, and the whole second operator (its guard,
+// sqrt and division).  Here the 32 lanes of a warp compute those for a chunk
+// of rows at once into shared memory, and lane 0 then runs the chain on what
+// depends on tv.  The operations and their operands are node_update2d's, so
+// the results are the same bits.
+constexpr int kChunk2 = 128;  // rows per precomputed chunk
+
+struct Pre2 {
+  double a1[kChunk2];    // dz * min slowness along z (t1d1 = tv + a1)
+  double t1d2[kChunk2];  // te + dx * min slowness along x
+  double c1[kChunk2];    // te + dx * vref (guard tv <= c1)
+  double b[kChunk2];     // dz * vref (guard te <= tv + b)
+  double p1[kChunk2];    // tev + te (ta = p1 - tv)
+  double p2[kChunk2];    // tev - te (tb = p2 + tv)
+  double x[kChunk2];     // 4 vref^2 (dz2i + dx2i), the radicand's constant term
+  double te[kChunk2], tev[kChunk2], vref[kChunk2];
+  double vv[kChunk2];    // vref * vref
+  double d3[kChunk2];    // the third operator's guard bound
+  double t2[kChunk2];    // the second operator's value, where it applies
+  unsigned char flags[kChunk2];  // 1: tev <= te; 2: the second operator applies
+};
+
+template <bool K>
+__device__ __forceinline__ void precompute_row2d(Pre2& P, int q, const double* tt,
+                                                 const double* slow, const Ops2& o, int i, int j,
+                                                 int sgnvz, int sgnvx, int sgntz, int sgntx,
+                                                 int NZ, int NX) {
+  const In2 in = load_in2(tt, slow, i, j, sgnvz, sgnvx, sgntz, sgntx, NZ, NX);
+  const double te = in.te, tev = in.tev;
+  P.a1[q] = o.dz * pmin(in.sz0, in.sz1);
+  P.t1d2[q] = te + o.dx * pmin(in.sx0, in.sx1);
+  const double vref = in.s2;
+  P.c1[q] = te + o.dx * vref;
+  P.b[q] = o.dz * vref;
+  P.p1[q] = tev + te;
+  P.p2[q] = tev - te;
+  const double vv = vref * vref;
+  P.vv[q] = vv;
+  P.x[q] = times4(vv) * o.s2;
+  P.te[q] = te;
+  P.tev[q] = tev;
+  P.vref[q] = vref;
+  P.d3[q] = div_by(o.dxx * vref, o.rhyp);
+  unsigned f = le2<K>(tev, te) ? 1u : 0u;
+  const double dte = te - tev;
+  if (le2<K>(dte, div_by(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, dte)) {
+    const double r = div_by(dte, o.rdz);
+    P.t2[q] = te + o.dx * sqrt(vv - r * r);
+    f |= 2u;
+  }
+  P.flags[q] = (unsigned char)f;
+}
+
+// node_update2d on precomputed row q: only the terms that involve tv.
+template <bool GRAD, bool K>
+__device__ __forceinline__ double chain_node2d(double* tt, uint8_t* rec, const Ops2& o,
+                                               const Source2& sp, const Pre2& P, int q, int i,
+                                               int j, int sgntz, int sgntx, int NX, double tv,
+                                               double t0) {
+  const long long n = (long long)i * NX + j;
+  const double t1d1 = tv + P.a1[q];
+  const double t1d2 = P.t1d2[q];
+  const double t1d = lt2<K>(t1d2, t1d1) ? t1d2 : t1d1;
+  double t2d = kBig;
+  const unsigned f = P.flags[q];
+  const double tev = P.tev[q];
+  const int di = i - sp.zsi, dj = j - sp.xsi;
+  if (di > kEpsin || di < -kEpsin || dj > kEpsin || dj < -kEpsin) {
+    if (le2<K>(tv, P.c1[q]) && le2<K>(P.te[q], tv + P.b[q]) && (f & 1u) && le2<K>(tev, tv)) {
+      const double ta = P.p1[q] - tv;
+      const double tb = P.p2[q] + tv;
+      const double d = ta - tb;
+      t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(P.x[q] - o.p2 * (d * d)), o.r2);
+    } else if (f & 2u) {
+      t2d = P.t2[q];
+    } else if (le2<K>(tv - tev, P.d3[q]) && lt2<K>(0.0, tv - tev)) {
+      const double r = div_by(tv - tev, o.rdx);
+      t2d = tv + o.dz * sqrt(P.vv[q] - r * r);
+    }
+  } else {
+    // spherical (factored) operator near the source, _fteik2d.py:144-171
+    const double te = P.te[q], vref = P.vref[q];
+    if (lt2<K>(tv, te + o.dx * vref) && lt2<K>(te, tv + o.dz * vref) && le2<K>(tev, te) &&
+        le2<K>(tev, tv)) {
+      double tzc, txc;
+      const double t0c = t_anad2(i, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero, tzc, txc);
+      const double tauv = tv - t_ana2(i - sgntz, j, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
+      const double taue = te - t_ana2(i, j - sgntx, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
+      const double tauev = tev - t_ana2(i - sgntz, j - sgntx, o.dz, o.dx, sp.zsa, sp.xsa, sp.vzero);
+      t2d = delta2(t2d, tauv, taue, tauev, t0c, tzc, txc, o.dzi, o.dxi, o.dz2i, o.dx2i,
+                   sp.vzero, vref, sgntz, sgntx);
+      if (t2d < tv || t2d < te) t2d = kBig;
+    }
+  }
+  double tnew = t0;
+  if (lt2<K>(t1d, tnew)) tnew = t1d;
+  if (lt2<K>(t2d, tnew)) tnew = t2d;
+  if (!eq2<K>(tnew, t0)) {
+    tt[n] = tnew;
+    if (GRAD) {
+      int a, bb;
+      if (eq2<K>(tnew, t1d1)) {
+        a = sgntz; bb = 0;
+      } else if (eq2<K>(tnew, t1d2)) {
+        a = 0; bb = sgntx;
+      } else {
+        a = sgntz; bb = sgntx;
+      }
+      rec[n] = (uint8_t)((a + 1) * 3 + (bb + 1));
+    }
+  }
+  return tnew;
+}
+
+// One pass over column j (rows i0, i0 + sgntz, ..., i1) by the whole warp.
+template <bool GRAD, bool K>
+__device__ __forceinline__ void warp_pass2d(Pre2& P, double* tt, uint8_t* rec, const double* slow,
+                                            const Ops2& o, const Source2& sp, int j, int i0,
+                                            int i1, int sgnvz, int sgnvx, int sgntz, int sgntx,
+                                            int NZ, int NX) {
+  const int lane = threadIdx.x & 31;
+  const int step = sgntz;
+  const int len = (i1 - i0) * step + 1;
+  double tv = 0.0;
+  if (lane == 0) tv = tt[(long long)(i0 - sgntz) * NX + j];
+  for (int c0 = 0; c0 < len; c0 += kChunk2) {
+    const int m = imin(kChunk2, len - c0);
+    for (int q = lane; q < m; q += 32)
+      precompute_row2d<K>(P, q, tt, slow, o, i0 + (c0 + q) * step, j, sgnvz, sgnvx, sgntz,
+                          sgntx, NZ, NX);
+    __syncwarp();
+    if (lane == 0) {
+      int i = i0 + c0 * step;
+      double t0n = tt[(long long)i * NX + j];
+      for (int q = 0; q < m; ++q, i += step) {
+        const double t0 = t0n;
+        if (q + 1 < m) t0n = tt[(long long)(i + step) * NX + j];
+        tv = chain_node2d<GRAD, K>(tt, rec, o, sp, P, q, i, j, sgntz, sgntx, NX, tv, t0);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <bool GRAD, bool K>
+__device__ __noinline__ void warp_sweeps2d(Pre2& P, double* tt, uint8_t* rec, const double* slow,
+                                           const Ops2& o, const Source2& sp, int nsweep, int NZ,
+                                           int NX) {
+  for (int sw = 0; sw < nsweep; ++sw) {
+    for (int j = 1; j < NX; ++j) {
+      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX);
+      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX);
+    }
+    for (int j = NX - 2; j >= 0; --j) {
+      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX);
+      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX);
+    }
+  }
+}
+
+// One warp per source (blockIdx.x): lane 0 runs the first propagation, the
+// warp checks it for non-finite values, then the sweeps run as above.
+template <bool GRAD>
+__global__ void __launch_bounds__(32) solve2d_warp_kernel(const double* slow, const double* src,
+                                                          int nz, int nx, int nsweep, Ops2 o,
+                                                          double* tt_all, uint8_t* rec_all,
+                                                          Source2* params, double* vzero_out,
+                                                          bool keys) {
+  __shared__ Pre2 P;
+  __shared__ Source2 sps;
+  const int s = blockIdx.x;
+  const int lane = threadIdx.x;
+  const int NZ = nz + 1, NX = nx + 1;
+  const long long nodes = (long long)NZ * NX;
+  double* tt = tt_all + (long long)s * nodes;
+  uint8_t* rec = GRAD ? rec_all + (long long)s * nodes : nullptr;
+  if (lane == 0) {
+    const Source2 sp = first_propagation2d<GRAD>(slow, src + 2 * s, nz, nx, o, tt, rec);
+    params[s] = sp;
+    vzero_out[s] = sp.vzero;
+    sps = sp;
+  }
+  __syncwarp();
+  const Source2 sp = sps;
+  bool finite = true;
+  for (int jj = lane; jj < NX; jj += 32)
+    for (int r = sp.zsi; r <= imin(sp.zsi + 1, NZ - 1); ++r)
+      finite = finite && is_finite(tt[(long long)r * NX + jj]);
+  for (int ii = lane; ii < NZ; ii += 32)
+    for (int c = sp.xsi; c <= imin(sp.xsi + 1, NX - 1); ++c)
+      finite = finite && is_finite(tt[(long long)ii * NX + c]);
+  finite = __all_sync(0xffffffffu, finite) && keys;
+  if (finite)
+    warp_sweeps2d<GRAD, true>(P, tt, rec, slow, o, sp, nsweep, NZ, NX);
+  else
+    warp_sweeps2d<GRAD, false>(P, tt, rec, slow, o, sp, nsweep, NZ, NX);
 }
 
 __global__ void fill2d_kernel(double* tt, uint8_t* rec, long long n) {
@@ -543,12 +765,25 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
   fill2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
   const int blocks = (nsrc + 31) / 32;
   const bool keys = option_value(kOptSweep2dKeys) != 0;
-  if (grad)
+  // A warp per source while every source's warp has an SM sub-partition to
+  // itself (its FP64 pipe is what the chain waits on); beyond that, one
+  // thread per source, where each warp instruction serves 32 chains.
+  const long long warp_opt = option_value(kOptSweep2dWarp);
+  const bool per_warp = warp_opt >= 0 ? warp_opt != 0 : nsrc <= 4 * sm_count();
+  if (per_warp) {
+    if (grad)
+      solve2d_warp_kernel<true><<<nsrc, 32, 0, st>>>(slow, src_dev, nz, nx, nsweep, o, tt, rec,
+                                                     params, vzero, keys);
+    else
+      solve2d_warp_kernel<false><<<nsrc, 32, 0, st>>>(slow, src_dev, nz, nx, nsweep, o, tt, rec,
+                                                      params, vzero, keys);
+  } else if (grad) {
     solve2d_kernel<true><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt, rec,
                                                  params, vzero, keys);
-  else
+  } else {
     solve2d_kernel<false><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt,
                                                   rec, params, vzero, keys);
+  }
   FTEIK_CHECK(cudaGetLastError());
   if (grad) {
     grad2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, params, nsrc, nz + 1, nx + 1,

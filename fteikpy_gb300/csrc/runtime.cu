@@ -26,7 +26,7 @@ void set_last_error(const char* fmt, ...) {
   va_end(ap);
 }
 
-static int sm_count() {
+int sm_count() {
   static int count = 0;
   if (count == 0) {
     int dev = 0;
@@ -61,7 +61,7 @@ int grid_for(long long n, int threads) {
   return (int)blocks;
 }
 
-static long long g_options[kOptCount] = {-1, -1, -1, -1, -1, -1, -1};
+static long long g_options[kOptCount] = {-1, -1, -1, -1, -1, -1, -1, -1};
 
 long long option_value(int opt) { return (opt >= 0 && opt < kOptCount) ? g_options[opt] : -1; }
 
@@ -116,6 +116,10 @@ extern "C" int fteik_set_option(const char* name, long long value) {
     g_options[kOptSweepTeam] = value < 0 ? -1 : (value ? 1 : 0);
     return kOk;
   }
+  if (std::strcmp(name, "sweep2d_warp") == 0) {
+    g_options[kOptSweep2dWarp] = value < 0 ? -1 : (value ? 1 : 0);
+    return kOk;
+  }
   if (std::strcmp(name, "sweep2d_keys") == 0) {
     g_options[kOptSweep2dKeys] = value < 0 ? -1 : (value ? 1 : 0);
     return kOk;
@@ -138,6 +142,7 @@ extern "C" int fteik_get_option(const char* name, long long* value) {
   else if (std::strcmp(name, "sweep_team") == 0) *value = g_options[kOptSweepTeam];
   else if (std::strcmp(name, "adjoint_chunk") == 0) *value = g_options[kOptAdjointChunk];
   else if (std::strcmp(name, "sweep2d_keys") == 0) *value = g_options[kOptSweep2dKeys];
+  else if (std::strcmp(name, "sweep2d_warp") == 0) *value = g_options[kOptSweep2dWarp];
   else return kInvalidArgument;
   return kOk;
 }

@@ -16,6 +16,9 @@ void set_last_error(const char* fmt, ...);
     if (err_ != cudaSuccess) return record_cuda_error(err_, #call); \
   } while (0)
 
+// Streaming multiprocessors of the current device (cached).
+int sm_count();
+
 // Blocks of `threads` threads that stay resident at once on the current
 // device for `kernel` (cached per kernel).
 int resident_blocks(const void* kernel, int threads, size_t smem = 0);
@@ -37,7 +40,8 @@ enum Option : int {
   kOptSweepTeam = 4,    // 3D team kernel (compacted operators): 1 on, 0 off
   kOptAdjointChunk = 5, // adjoint reverse sweeps: steps between progress publications
   kOptSweep2dKeys = 6,  // 2D sweeps: 0 forces IEEE comparisons (else integer keys when exact)
-  kOptCount = 7,
+  kOptSweep2dWarp = 7,  // 2D sweeps: 1 one warp per source, 0 one thread per source
+  kOptCount = 8,
 };
 long long option_value(int opt);
 

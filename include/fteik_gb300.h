@@ -55,6 +55,9 @@ int fteik_kernel_timing(int on);
  * "sweep2d_keys": 0 makes the 2D sweeps compare with IEEE comparisons
  * throughout (by default they use integer order keys for every source whose
  * first propagation left only finite values, where the two agree).
+ * "sweep2d_warp": 1 runs each 2D source on a warp (the warp precomputes the
+ * terms of each column that do not depend on the previous node, one lane
+ * runs the chain; the default up to 4 sources per SM), 0 on one thread.
  * Results are identical for every setting.
  * fteik_get_option reads a knob back. */
 int fteik_set_option(const char* name, long long value);

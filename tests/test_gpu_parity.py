@@ -251,18 +251,23 @@ def test_solve3d_batched_equals_single(nsrc):
     ],
 )
 @pytest.mark.parametrize("keys", [-1, 0])
-def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys):
-    """Both comparison paths of the 2D sweeps (integer keys, the default for
-    sources whose first propagation is finite; IEEE comparisons, forced by
-    the "sweep2d_keys" option) against the oracle, bit for bit."""
+@pytest.mark.parametrize("warp", [1, 0])
+def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys, warp):
+    """Both 2D kernels (one warp per source with the rows' tv-independent terms
+    precomputed by the warp, the default for few sources; one thread per
+    source) and both comparison paths (integer keys, the default for sources
+    whose first propagation is finite; IEEE comparisons) against the oracle,
+    bit for bit."""
     from fteikpy_gb300 import _lib
 
     lib = _lib.load()
     assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
+    assert lib.fteik_set_option(b"sweep2d_warp", warp) == 0
     try:
         _solve2d_bitwise_case(shape, d, nsrc, nsweep, seed)
     finally:
         lib.fteik_set_option(b"sweep2d_keys", -1)
+        lib.fteik_set_option(b"sweep2d_warp", -1)
 
 
 def _solve2d_bitwise_case(shape, d, nsrc, nsweep, seed):
@@ -453,7 +458,8 @@ def test_rays_bitwise_vs_oracle_on_exact_and_inexact_axes(nd, d, og, stepsize):
 
 
 @pytest.mark.parametrize("keys", [-1, 0])
-def test_solve2d_sources_on_the_far_boundaries(keys):
+@pytest.mark.parametrize("warp", [1, 0])
+def test_solve2d_sources_on_the_far_boundaries(keys, warp):
     """Sources on the bottom and right model edges (where the reference's first
     propagation divides by zero, _fteik2d.py:444-445) next to interior ones,
     in one launch: both comparison paths against the oracle, bit for bit."""
@@ -468,10 +474,12 @@ def test_solve2d_sources_on_the_far_boundaries(keys):
     src = np.array([[zmax, 123.3], [55.5, 100.1], [zmax, xmax], [0.0, 77.7], [133.0, xmax],
                     [zmax, 0.0], [211.1, 150.0]])
     assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
+    assert lib.fteik_set_option(b"sweep2d_warp", warp) == 0
     try:
         tts = fp.Eikonal2D(v, d).solve(src, nsweep=2, return_gradient=True)
     finally:
         lib.fteik_set_option(b"sweep2d_keys", -1)
+        lib.fteik_set_option(b"sweep2d_warp", -1)
     tt_o, tg_o, vz_o = O.solve2d(1.0 / v, d, src, 2, True)
     assert bitwise(np.stack([t.grid for t in tts]), tt_o)
     assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)

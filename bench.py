@@ -343,7 +343,8 @@ def run_config1(args):
         "analytic_linear_gradient_rel_err": {"max": float(rel.max()), "median": float(np.median(rel)),
                                              "excluding": "nodes within 5 cells of the source"},
         "note": "the reference's 2D sweep is one serial dependence chain; a single 2D source "
-                "runs on one GPU thread",
+                "runs on one warp: the warp precomputes each column's terms that do not "
+                "depend on the previous node, one lane runs the chain",
     }))
     return 0
 

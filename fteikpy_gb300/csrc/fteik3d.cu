@@ -997,27 +997,37 @@ __global__ void fill3d_batch_kernel(const Model3* models, const Job3* jobs) {
   }
 }
 
-// Gradient post-pass, _fteik3d.py:464-488.  The 8 nodes around the source
-// start from the analytic derivatives they were initialised with
-// (_fteik3d.py:453-456); every other node starts from zero.
-__device__ __forceinline__ void grad3d_node(const double* tt, const uint8_t* rec, long long n,
-                                            const Source3& p, int NX, int NY, const Ops3& o,
-                                            double* g) {
+// Gradient post-pass, _fteik3d.py:464-488, for node n = (i, j, k).  The 8
+// nodes around the source start from the analytic derivatives they were
+// initialised with (_fteik3d.py:453-456); every other node starts from zero.
+// The reference's `sgn * (t - t_upwind)` with sgn = +-1 is the difference or
+// its negation (the same bits), and `gn > 0` holds exactly when gn's bit
+// pattern is positive and not NaN's (gn is a square root).
+__device__ __forceinline__ void grad3d_node_at(const double* tt, const uint8_t* rec, long long n,
+                                               int i, int j, int k, const Source3& p, int NX,
+                                               int NY, const Ops3& o, double* g) {
   const long long NXY = (long long)NX * NY;
-  const int i = (int)(n / NXY);
-  const int j = (int)((n - (long long)i * NXY) / NY);
-  const int k = (int)(n - (long long)i * NXY - (long long)j * NY);
   double g0 = 0.0, g1 = 0.0, g2 = 0.0;
   if ((unsigned)(i - p.zsi) <= 1u && (unsigned)(j - p.xsi) <= 1u && (unsigned)(k - p.ysi) <= 1u)
     t_anad3(i, j, k, o, p, g0, g1, g2);
   const int code = rec[n];
   const int cz = code / 9 - 1, cx = (code / 3) % 3 - 1, cy = code % 3 - 1;
   const double tq = tt[n];
-  if (cz != 0) g0 = div_by((double)cz * (tq - tt[n - cz * NXY]), o.rdz);
-  if (cx != 0) g1 = div_by((double)cx * (tq - tt[n - (long long)cx * NY]), o.rdx);
-  if (cy != 0) g2 = div_by((double)cy * (tq - tt[n - cy]), o.rdy);
+  if (cz != 0) {
+    const double d = tq - tt[n - cz * NXY];
+    g0 = div_by(cz > 0 ? d : -d, o.rdz);
+  }
+  if (cx != 0) {
+    const double d = tq - tt[n - (long long)cx * NY];
+    g1 = div_by(cx > 0 ? d : -d, o.rdx);
+  }
+  if (cy != 0) {
+    const double d = tq - tt[n - cy];
+    g2 = div_by(cy > 0 ? d : -d, o.rdy);
+  }
   const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
-  if (gn > 0.0) {
+  const long long gb = __double_as_longlong(gn);
+  if (gb > 0 && gb <= 0x7ff0000000000000LL) {
     g0 /= gn;
     g1 /= gn;
     g2 /= gn;
@@ -1025,6 +1035,19 @@ __device__ __forceinline__ void grad3d_node(const double* tt, const uint8_t* rec
   g[3 * n] = g0;
   g[3 * n + 1] = g1;
   g[3 * n + 2] = g2;
+}
+
+// One thread per node (grid-stride).  The kernel is bound by its FP64 work
+// (three constant divisions, a square root and three IEEE divisions per
+// node); the index arithmetic runs beside it on the integer pipe.
+__device__ __forceinline__ void grad3d_node(const double* tt, const uint8_t* rec, long long n,
+                                            const Source3& p, int NX, int NY, const Ops3& o,
+                                            double* g) {
+  const long long NXY = (long long)NX * NY;
+  const int i = (int)(n / NXY);
+  const int j = (int)((n - (long long)i * NXY) / NY);
+  const int k = (int)(n - (long long)i * NXY - (long long)j * NY);
+  grad3d_node_at(tt, rec, n, i, j, k, p, NX, NY, o, g);
 }
 
 __global__ void grad3d_kernel(const double* tt, const uint8_t* rec, const Source3* params,

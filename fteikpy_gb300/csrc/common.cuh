@@ -101,6 +101,32 @@ __device__ __forceinline__ double div_by(double x, const Recip& r) {
   return __fma_rn(rem, r.hi, q);                     // Markstein correction
 }
 
+// RN(a / b) for several numerators sharing one divisor b: y = RN(1/b) and
+// lo = RN((1 - b*y) * y) make y + lo a reciprocal of b accurate to about
+// 2^-104, so q = a*y + a*lo (one FMA) is faithful, and the same Markstein
+// correction as div_by rounds it correctly.  Numerators that are zero (the
+// quotient keeps their sign), non-finite, or so small that the quotient
+// could leave the normal range take the IEEE division.
+struct SharedRecip {
+  double b, y, lo;
+};
+__device__ __forceinline__ SharedRecip shared_recip(double b) {
+  SharedRecip r;
+  r.b = b;
+  r.y = 1.0 / b;
+  r.lo = __dmul_rn(__fma_rn(-b, r.y, 1.0), r.y);
+  return r;
+}
+__device__ __forceinline__ double div_shared(double a, const SharedRecip& r) {
+  const long long ba = __double_as_longlong(a) & 0x7fffffffffffffffLL;
+  const int ea = (int)(ba >> 52), eb = (int)((__double_as_longlong(r.b) >> 52) & 0x7ff);
+  if (ba == 0) return a;
+  if (ea == 0x7ff || ea - eb < -900 || eb < 64 || eb > 1983) return a / r.b;
+  const double q = __fma_rn(a, r.y, __dmul_rn(a, r.lo));
+  const double rem = __fma_rn(-q, r.b, a);
+  return __fma_rn(rem, r.y, q);
+}
+
 // ---- misc ------------------------------------------------------------------------
 
 __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }

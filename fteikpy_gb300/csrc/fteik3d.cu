@@ -1028,9 +1028,11 @@ __device__ __forceinline__ void grad3d_node_at(const double* tt, const uint8_t* 
   const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
   const long long gb = __double_as_longlong(gn);
   if (gb > 0 && gb <= 0x7ff0000000000000LL) {
-    g0 /= gn;
-    g1 /= gn;
-    g2 /= gn;
+    // g /= gn, one correctly rounded quotient per component
+    const SharedRecip rn = shared_recip(gn);
+    g0 = div_shared(g0, rn);
+    g1 = div_shared(g1, rn);
+    g2 = div_shared(g2, rn);
   }
   g[3 * n] = g0;
   g[3 * n + 1] = g1;
@@ -1038,8 +1040,9 @@ __device__ __forceinline__ void grad3d_node_at(const double* tt, const uint8_t* 
 }
 
 // One thread per node (grid-stride).  The kernel is bound by its FP64 work
-// (three constant divisions, a square root and three IEEE divisions per
-// node); the index arithmetic runs beside it on the integer pipe.
+// (three constant divisions, a square root, a reciprocal and three
+// corrected quotients per node); the index arithmetic runs beside it on the
+// integer pipe.
 __device__ __forceinline__ void grad3d_node(const double* tt, const uint8_t* rec, long long n,
                                             const Source3& p, int NX, int NY, const Ops3& o,
                                             double* g) {

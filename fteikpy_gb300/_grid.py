@@ -69,7 +69,10 @@ class _TraveltimeMixin:
 
     def _raytrace(self, points, stepsize, max_step, honor_grid):
         nd = self._ndim
-        self.gradient  # raises ValueError without gradients, as the reference
+        if self._gradient is None:  # the reference's error (fteikpy/_grid.py:270-273)
+            raise ValueError(
+                "no gradient grid, use option `return_gradient` to return gradient grids"
+            )
         if honor_grid or not stepsize:
             stepsize = np.min(self._gridsize)
         if not max_step:

@@ -38,6 +38,17 @@ class _TraveltimeMixin:
             self._gradient = g
         return g.contiguous()
 
+    def _device_source(self):
+        """[source coordinates..., vzero] as a CUDA tensor, uploaded once (the
+        per-call interpolation and ray tracing read them on the device)."""
+        c = getattr(self, "_source_cache", None)
+        if c is None:
+            host = np.append(np.asarray(self._source, dtype=np.float64).reshape(-1),
+                             float(self._vzero))
+            c = _device.to_device(host)
+            self._source_cache = c
+        return c
+
     def _vinterp(self, points, fill_value):
         nd = self._ndim
         pts = np.asarray(points, dtype=np.float64)
@@ -47,8 +58,8 @@ class _TraveltimeMixin:
         tt = self._device_grid().contiguous()
         ax = self._device_axes()
         q = _device.to_device(pts2)
-        src = _device.to_device(self._source.reshape(1, nd))
-        vz = _device.to_device(np.array([float(self._vzero)]))
+        sv = self._device_source()
+        src, vz = sv[:nd], sv[nd:]
         out = torch.empty(len(pts2), dtype=torch.float64, device=q.device)
         if nd == 3:
             rc = lib.fteik_vinterp3d(
@@ -81,7 +92,8 @@ class _TraveltimeMixin:
         pts = np.asarray(points, dtype=np.float64)
         rays = trace_rays(
             nd, self._device_axes(), self._device_gradient(), None, pts.reshape(-1, nd),
-            self._source.reshape(1, nd), float(stepsize), int(max_step), bool(honor_grid),
+            self._device_source()[:nd].reshape(1, nd), float(stepsize), int(max_step),
+            bool(honor_grid),
         )
         return rays[0] if pts.ndim == 1 else rays
 

@@ -523,26 +523,37 @@ __device__ __forceinline__ void precompute_row2d(Pre2& P, int q, const double* t
   P.flags[q] = (unsigned char)f;
 }
 
+// The precomputed terms the chain reads on every node, loaded into registers
+// one node ahead (the rarer branches read shared memory directly).
+struct Row2 {
+  double a1, t1d2, c1, b, p1, p2, x, te, tev;
+  unsigned flags;
+};
+__device__ __forceinline__ Row2 load_row2(const Pre2& P, int q) {
+  return Row2{P.a1[q], P.t1d2[q], P.c1[q], P.b[q], P.p1[q], P.p2[q],
+              P.x[q],  P.te[q],   P.tev[q], P.flags[q]};
+}
+
 // node_update2d on precomputed row q: only the terms that involve tv.
 template <bool GRAD, bool K>
 __device__ __forceinline__ double chain_node2d(double* tt, uint8_t* rec, const Ops2& o,
-                                               const Source2& sp, const Pre2& P, int q, int i,
-                                               int j, int sgntz, int sgntx, int NX, double tv,
-                                               double t0) {
+                                               const Source2& sp, const Pre2& P, const Row2& R,
+                                               int q, int i, int j, int sgntz, int sgntx, int NX,
+                                               double tv, double t0) {
   const long long n = (long long)i * NX + j;
-  const double t1d1 = tv + P.a1[q];
-  const double t1d2 = P.t1d2[q];
+  const double t1d1 = tv + R.a1;
+  const double t1d2 = R.t1d2;
   const double t1d = lt2<K>(t1d2, t1d1) ? t1d2 : t1d1;
   double t2d = kBig;
-  const unsigned f = P.flags[q];
-  const double tev = P.tev[q];
+  const unsigned f = R.flags;
+  const double tev = R.tev;
   const int di = i - sp.zsi, dj = j - sp.xsi;
   if (di > kEpsin || di < -kEpsin || dj > kEpsin || dj < -kEpsin) {
-    if (le2<K>(tv, P.c1[q]) && le2<K>(P.te[q], tv + P.b[q]) && (f & 1u) && le2<K>(tev, tv)) {
-      const double ta = P.p1[q] - tv;
-      const double tb = P.p2[q] + tv;
+    if (le2<K>(tv, R.c1) && le2<K>(R.te, tv + R.b) && (f & 1u) && le2<K>(tev, tv)) {
+      const double ta = R.p1 - tv;
+      const double tb = R.p2 + tv;
       const double d = ta - tb;
-      t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(P.x[q] - o.p2 * (d * d)), o.r2);
+      t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt(R.x - o.p2 * (d * d)), o.r2);
     } else if (f & 2u) {
       t2d = P.t2[q];
     } else if (le2<K>(tv - tev, P.d3[q]) && lt2<K>(0.0, tv - tev)) {
@@ -551,7 +562,7 @@ __device__ __forceinline__ double chain_node2d(double* tt, uint8_t* rec, const O
     }
   } else {
     // spherical (factored) operator near the source, _fteik2d.py:144-171
-    const double te = P.te[q], vref = P.vref[q];
+    const double te = R.te, vref = P.vref[q];
     if (lt2<K>(tv, te + o.dx * vref) && lt2<K>(te, tv + o.dz * vref) && le2<K>(tev, te) &&
         le2<K>(tev, tv)) {
       double tzc, txc;
@@ -604,10 +615,15 @@ __device__ __forceinline__ void warp_pass2d(Pre2& P, double* tt, uint8_t* rec, c
     if (lane == 0) {
       int i = i0 + c0 * step;
       double t0n = tt[(long long)i * NX + j];
+      Row2 rn = load_row2(P, 0);
       for (int q = 0; q < m; ++q, i += step) {
         const double t0 = t0n;
-        if (q + 1 < m) t0n = tt[(long long)(i + step) * NX + j];
-        tv = chain_node2d<GRAD, K>(tt, rec, o, sp, P, q, i, j, sgntz, sgntx, NX, tv, t0);
+        const Row2 r = rn;
+        if (q + 1 < m) {
+          t0n = tt[(long long)(i + step) * NX + j];
+          rn = load_row2(P, q + 1);
+        }
+        tv = chain_node2d<GRAD, K>(tt, rec, o, sp, P, r, q, i, j, sgntz, sgntx, NX, tv, t0);
       }
     }
     __syncwarp();

@@ -9,8 +9,9 @@
 // match finite differences of the solver.  The forward solve therefore keeps a
 // tape (fteik3d_solve_tape): for every sweep, the code of the operator that
 // changed each node (the reference's ttsgn, _fteik3d.py:166-200) and the value
-// it replaced.  Going back through the sweeps in reverse hyperplane order, a
-// node first collects the adjoint its readers of that sweep sent it, then, if
+// it replaced.  Going back through the sweeps, each undone against its own
+// direction (so that a node comes after every node that read it), a node
+// first collects the adjoint its readers of that sweep sent it, then, if
 // the sweep changed it, recomputes its operator's partials from the values it
 // read (_fteik3d.py:76-159; no saved intermediates), sends the adjoint on to
 // those inputs, books the slowness term, and restores its previous value.

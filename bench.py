@@ -12,14 +12,18 @@ Printed JSON line (rank 0):
   e2e       the same step through the drop-in Python API from host arrays
             (velocity upload, solve, rays and first-arrival picks copied back)
   plain     the same grid solved one source per launch (the "plain" solve)
-  roofline  the sweep kernel's FP64 rate against the FP64 peak measured in
-            this run, with its HBM rate beside it
-  cpu_baseline  the CPU oracle (C restatement of the reference, OpenMP over
-            all host cores) on a bounded sample of the same workload
+  roofline  the sweep kernel's executed FP64 lane instructions per second
+            against the FP64 pipe's peak measured in this run, with the
+            reference's algorithmic operation count and the HBM rate beside it
+  cpu_baseline  the reference's kernels on the host CPU (the oracle's C
+            restatement, built for timing with the reference's numba
+            floating-point licences, OpenMP over all host cores) on a bounded
+            sample of the same workload
 
-``--impl reference`` times the reference's CPU implementation instead: numba is
-not installed on these hosts, so this is the oracle's C restatement with all
-host threads (the reference's own pure-Python mode is ~1e4x slower still).
+``--impl reference`` times that CPU implementation alone: numba is not
+installed on these hosts, so the reference's kernels run as the oracle's C
+restatement with all host threads (the reference's own pure-Python mode is
+~1e4x slower still).
 """
 
 import argparse
@@ -43,10 +47,13 @@ NREC = 400
 NSWEEP = 2
 FLOP_PER_UPDATE = 160  # algorithmic FP64 operations of one 3D node update
 BYTES_PER_UPDATE = 25  # slowness + tt read + tt write (8 B each) + 1 B branch record
-# DRAM bytes (read + write) per node update of the team sweep kernel, measured
-# by ncu on the 192-source 64x128x128 case (profiles/sweep3d_team_small_full.md:
-# 87.147 GB + 9.593 GB for 3.221 G updates); the full launch is scaled from it.
-TRAFFIC_BYTES_PER_UPDATE = (87.147e9 + 9.593e9) / 3221225472
+# Per node update of the team sweep kernel on the layered benchmark model, from
+# one ncu capture of that kernel on the 192-source 64x128x128 case: executed
+# FP64 thread instructions (DADD + DMUL + DFMA, one per active lane) and DRAM
+# bytes read + written. The bench scales both by the updates of the timed
+# launch.
+TEAM_FP64_LANE_OPS_PER_UPDATE = 49.47
+TEAM_DRAM_BYTES_PER_UPDATE = (87.147e9 + 9.593e9) / 3221225472
 
 
 def smooth2d(rng, shape, sigma):
@@ -205,10 +212,17 @@ def rank_sources(rank, shape=None):
     return surface_sources(shape, seed=7 + 1000 * rank)
 
 
+CPU_BUILD = ("the reference's kernels restated in C (numba is not installed on this host), "
+             "built for timing with the reference's numba floating-point licences "
+             "(gcc -O3, FMA contraction, reciprocal multiplication, no signed zeros), "
+             "OpenMP over sources")
+
+
 def cpu_sample(nthreads=None, nsrc=None, shape=None):
-    """Time the CPU oracle (all host cores, OpenMP over sources) on a bounded
-    sample of the workload: as many sources as threads, solved with gradients,
-    plus their rays. Returns (shots/s, threads, sample description)."""
+    """Time the CPU reference path (the oracle's timing build, all host cores,
+    OpenMP over sources) on a bounded sample of the workload: as many sources
+    as threads, solved with gradients, plus their rays. Returns (shots/s,
+    threads, sample description)."""
     from oracle import oracle as O
 
     shape = shape or SHAPE
@@ -217,16 +231,16 @@ def cpu_sample(nthreads=None, nsrc=None, shape=None):
     v = layered_model(shape)
     src = surface_sources(shape)[:nsrc]
     rec = surface_receivers(shape)
-    O.lib()
+    O.lib(fast=True)
     t0 = time.perf_counter()
-    tt, tg, vz = O.solve3d(1.0 / v, D, src, NSWEEP, True, nthreads=nthreads)
+    tt, tg, vz = O.solve3d(1.0 / v, D, src, NSWEEP, True, nthreads=nthreads, fast=True)
     ax = O.axes(tt.shape[1:], D, np.zeros(3))
     max_dist = 2.0 * sum((n * h) ** 2 for n, h in zip(tt.shape[1:], D)) ** 0.5
     for s in range(nsrc):
-        O.raytrace(ax, tg[s], rec, src[s], min(D), int(max_dist / min(D)), False)
+        O.raytrace(ax, tg[s], rec, src[s], min(D), int(max_dist / min(D)), False, fast=True)
     dt = time.perf_counter() - t0
     desc = (f"{nsrc} of the {NSRC} sources on the {shape[0]}x{shape[1]}x{shape[2]} grid "
-            f"(solve with gradients + {NREC} rays each), {nthreads} threads")
+            f"(solve with gradients + {NREC} rays each), {nthreads} threads; {CPU_BUILD}")
     return nsrc / dt, nthreads, desc
 
 
@@ -265,8 +279,7 @@ def run_reference(args):
             "unit": "shots/s",
             "cores": nthreads,
             "kind": "port",
-            "sample": desc + "; numba is not installed on this host, so the reference's "
-            "kernels run as the oracle's line-by-line C restatement (gcc -O2, OpenMP)",
+            "sample": desc,
         },
         "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -289,6 +302,34 @@ def workload_config():
     }
 
 
+def config1_models(shape=(200, 300), d=(10.0, 10.0), seed=1):
+    """The plain 2D workload: v(z) = 1500 + 0.6 z (cell centres) times
+    (1 + 0.1 p), p seeded N(0,1) noise Gaussian-smoothed with sigma = 8 cells
+    and rescaled to [-1, 1]. Returns (v, v0 = the p = 0 model, source, d)."""
+    from scipy.ndimage import gaussian_filter
+
+    nz, nx = shape
+    rng = np.random.default_rng(seed)
+    p = gaussian_filter(rng.standard_normal((nz, nx)), 8.0)
+    p = 2.0 * (p - p.min()) / (p.max() - p.min()) - 1.0
+    zc = (np.arange(nz) + 0.5) * d[0]
+    v0 = (1500.0 + 0.6 * zc)[:, None] * np.ones((nz, nx))
+    return v0 * (1.0 + 0.1 * p), v0, np.array([5.3, 1234.7]), d
+
+
+def linear_gradient_times(shape, d, src, v_top=1500.0, g=0.6, min_cells=5):
+    """Analytic first-arrival times T = arccosh(1 + g^2 r^2 / (2 v_s v)) / g of
+    the velocity v(z) = v_top + g z at the nodes of a grid (2D or 3D, z
+    first), and the mask of nodes farther than ``min_cells`` cells from the
+    source (the near-source nodes start from the solver's own analytic
+    initialisation)."""
+    axes = np.meshgrid(*[np.arange(n + 1) * h for n, h in zip(shape, d)], indexing="ij")
+    r2 = sum((a - s) ** 2 for a, s in zip(axes, src))
+    vs, vn = v_top + g * src[0], v_top + g * axes[0]
+    t = np.arccosh(1.0 + g * g * r2 / (2.0 * vs * vn)) / g
+    return t, r2 > (min_cells * min(d)) ** 2
+
+
 def run_config1(args):
     """Plain 2D solve (the reference's CPU-runnable case): 200 x 300 cells at
     10 m, v(z) = 1500 + 0.6 z times (1 + 0.1 p), p seeded N(0,1) noise smoothed
@@ -299,16 +340,8 @@ def run_config1(args):
 
     import fteikpy_gb300 as fp
     from oracle import oracle as O
-    from scipy.ndimage import gaussian_filter
 
-    nz, nx, d = 200, 300, (10.0, 10.0)
-    rng = np.random.default_rng(1)
-    p = gaussian_filter(rng.standard_normal((nz, nx)), 8.0)
-    p = 2.0 * (p - p.min()) / (p.max() - p.min()) - 1.0
-    zc = (np.arange(nz) + 0.5) * d[0]
-    v0 = (1500.0 + 0.6 * zc)[:, None] * np.ones((nz, nx))
-    v = v0 * (1.0 + 0.1 * p)
-    src = np.array([5.3, 1234.7])
+    v, v0, src, d = config1_models()
     eik = fp.Eikonal2D(v, d)
     for _ in range(max(args.warmup, 1)):
         eik.solve(src, nsweep=2)
@@ -319,26 +352,22 @@ def run_config1(args):
         tt = eik.solve(src, nsweep=2)
         g = tt.grid
         times.append(time.perf_counter() - t0)
-    t0 = time.perf_counter()
     tto, _, _ = O.solve2d(1.0 / v, d, [src], 2, False, nthreads=1)
-    cpu = time.perf_counter() - t0
     same = bool(np.array_equal(g, tto[0]))
+    O.solve2d(1.0 / v, d, [src], 2, False, nthreads=1, fast=True)
+    t0 = time.perf_counter()
+    O.solve2d(1.0 / v, d, [src], 2, False, nthreads=1, fast=True)
+    cpu = time.perf_counter() - t0
     # analytic linear-gradient traveltime for p = 0 (velocity at cell centres)
     t_lin = fp.Eikonal2D(v0, d).solve(src, nsweep=2).grid
-    gz = 0.6
-    zn = np.arange(nz + 1)[:, None] * d[0]
-    xn = np.arange(nx + 1)[None, :] * d[1]
-    r2 = (zn - src[0]) ** 2 + (xn - src[1]) ** 2
-    vs, vn = 1500.0 + gz * src[0], 1500.0 + gz * zn
-    t_ana = np.arccosh(1.0 + gz**2 * r2 / (2.0 * vs * vn)) / gz
-    far = r2 > (5 * d[0]) ** 2
+    t_ana, far = linear_gradient_times(v.shape, d, src)
     rel = np.abs(t_lin - t_ana)[far] / t_ana[far]
     print(json.dumps({
         "config": 1,
         "metric": "2D plain solve time (200x300, nsweep=2, one off-grid source)",
         "value": 1e3 * float(np.median(times)), "unit": "ms", "higher_is_better": False,
         "cpu_baseline": {"value": 1e3 * cpu, "unit": "ms", "cores": 1, "kind": "port",
-                         "sample": "the same solve, C oracle, 1 thread"},
+                         "sample": "the same solve, 1 thread; " + CPU_BUILD},
         "parity_bitwise_vs_oracle": same,
         "analytic_linear_gradient_rel_err": {"max": float(rel.max()), "median": float(np.median(rel)),
                                              "excluding": "nodes within 5 cells of the source"},
@@ -403,18 +432,18 @@ def run_config2(args):
     return 0
 
 
-def uneven_models(nmodel=64, seed=44):
+def uneven_models(nmodel=64, seed=44, sizes=(32, 160)):
     """Config-4 batch: per model, cell counts drawn uniformly from [32, 160]
-    per axis, one grid spacing drawn from [5, 20] m, velocity 1500..2500 m/s at the
-    top plus a 0.3..1.0 1/s gradient, times (1 + 0.1 p) with p seeded normal
-    noise Gaussian-smoothed (sigma 3 cells) and rescaled to [-1, 1], and 1..16
-    seeded off-grid sources anywhere in the model."""
+    per axis (``sizes``), one grid spacing drawn from [5, 20] m, velocity
+    1500..2500 m/s at the top plus a 0.3..1.0 1/s gradient, times (1 + 0.1 p)
+    with p seeded normal noise Gaussian-smoothed (sigma 3 cells) and rescaled
+    to [-1, 1], and 1..16 seeded off-grid sources anywhere in the model."""
     from scipy.ndimage import gaussian_filter
 
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(nmodel):
-        shape = tuple(int(x) for x in rng.integers(32, 161, 3))
+        shape = tuple(int(x) for x in rng.integers(sizes[0], sizes[1] + 1, 3))
         d = (float(rng.uniform(5.0, 20.0)),) * 3
         z = (np.arange(shape[0]) + 0.5) * d[0]
         v = (rng.uniform(1500.0, 2500.0) + rng.uniform(0.3, 1.0) * z)[:, None, None]
@@ -647,7 +676,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--plain-sources", type=int, default=8,
+                    help="sources solved one per launch for the plain leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end API timing")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-source-per-launch timing")
@@ -746,30 +777,44 @@ def main():
     shots = NSRC * world / (ms_step * 1e-3)
     sweep = float(np.mean(sweep_ms))
 
-    # roofline of the sweep kernel (one launch = all sweeps of all sources)
+    # roofline of the sweep kernel (one launch = all sweeps of all sources).
+    # The FP64 pipe's peak is measured in this run by a DFMA loop
+    # (fteik_fp64_peak, 2 flops per DFMA lane); in FP64 lane instructions per
+    # second it is half that. The kernel's executed lane instructions per
+    # update come from an ncu capture of the same kernel (see the constant).
     kernel_name = lib.fteik_last_sweep_kernel().decode()
     updates = updates_per_source() * NSRC
     scratch = torch.empty(152 * 8 * 256, dtype=torch.float64, device=dev)
     peak = __import__("ctypes").c_double()
     lib.fteik_fp64_peak(_device.ptr(scratch), 152 * 8, 20000, peak, _device.stream())
-    achieved_tf = updates * FLOP_PER_UPDATE / (sweep * 1e-3) / 1e12
-    peak_tf = peak.value / 1e12
+    peak_lane_ops = peak.value / 2.0
+    executed_lane_ops = updates * TEAM_FP64_LANE_OPS_PER_UPDATE / (sweep * 1e-3)
+    algorithmic_ops = updates * FLOP_PER_UPDATE / (sweep * 1e-3)
     hbm_gbs = updates * BYTES_PER_UPDATE / (sweep * 1e-3) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm_peak = json.load(open(peaks_path))["hbm_gbs"] if os.path.exists(peaks_path) else 6800.0
-    traffic = TRAFFIC_BYTES_PER_UPDATE * updates
+    traffic = TEAM_DRAM_BYTES_PER_UPDATE * updates
 
-    # plain: one source per launch on the same grid
-    plain_n = 0 if args.no_plain else 4
-    torch.cuda.synchronize()
-    p0 = time.perf_counter()
-    for s in range(plain_n):
-        tt1, tg1, _ = _solver.solve3d_device(slow, D, src[s:s + 1], NSWEEP, True)
-        trace_rays_device(3, axes, tg1, None, _device.to_device(rec), src_dev[s:s + 1], min(D),
-                          max_step, False)
+    # plain: one source per launch on the same grid, each with its 400 rays,
+    # timed with CUDA events on the launching stream
+    plain_n = 0 if args.no_plain else args.plain_sources
+    plain_ms = None
+    if plain_n:
+        rec_dev = _device.to_device(rec)
+        tt1, tg1, _ = _solver.solve3d_device(slow, D, src[:1], NSWEEP, True)  # warm
         del tt1, tg1
-    torch.cuda.synchronize()
-    plain_ms = 1e3 * (time.perf_counter() - p0) / max(plain_n, 1)
+        torch.cuda.synchronize()
+        pe0 = torch.cuda.Event(enable_timing=True)
+        pe1 = torch.cuda.Event(enable_timing=True)
+        pe0.record()
+        for s in range(plain_n):
+            tt1, tg1, _ = _solver.solve3d_device(slow, D, src[s:s + 1], NSWEEP, True)
+            trace_rays_device(3, axes, tg1, None, rec_dev, src_dev[s:s + 1], min(D), max_step,
+                              False)
+            del tt1, tg1
+        pe1.record()
+        torch.cuda.synchronize()
+        plain_ms = pe0.elapsed_time(pe1) / plain_n
     plain_shots = 1e3 / plain_ms if plain_n else None
 
     # e2e through the drop-in API from host arrays
@@ -825,29 +870,42 @@ def main():
                 "value": plain_shots,
                 "unit": "shots/s",
                 "ms_per_shot": plain_ms,
-                "what": "same grid, one source per solve launch (+ its 400 rays)",
+                "sources": plain_n,
+                "what": "same grid, one source per solve launch (+ its 400 rays), CUDA events",
                 "batched_over_plain": (shots / world / plain_shots) if plain_shots else None,
             },
             "roofline": {
                 "bound": "fp64",
                 "kernel": kernel_name,
-                "achieved": achieved_tf,
-                "peak": peak_tf,
-                "unit": "TFLOP/s",
-                "frac": achieved_tf / peak_tf,
-                "flop_per_update": FLOP_PER_UPDATE,
-                "peak_source": "DFMA loop measured in this run (fteik_fp64_peak)",
-                "note": "algorithmic work counts every node update of the reference's loops; "
-                        "the kernel skips the 2D/3D operators of nodes that provably keep "
-                        "their value (exact, bitwise-tested), so frac can pass 1; ncu on the "
-                        "192-source case: FP64 pipe 77% busy, useful FP64 lane work 66% of "
-                        "peak",
+                "unit": "T FP64 lane-instructions/s",
+                "achieved": executed_lane_ops / 1e12,
+                "peak": peak_lane_ops / 1e12,
+                "frac": executed_lane_ops / peak_lane_ops,
+                "executed_lane_ops_per_update": TEAM_FP64_LANE_OPS_PER_UPDATE,
+                "executed_source": "ncu sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on "
+                                   "of this kernel on the 192-source 64x128x128 layered case, "
+                                   "per node update, times the updates of this launch",
+                "peak_source": "DFMA loop measured in this run (fteik_fp64_peak): "
+                               "%.4f TFLOP/s counting 2 flops per DFMA lane, i.e. %.4f T "
+                               "lane-instructions/s" % (peak.value / 1e12, peak_lane_ops / 1e12),
+                "algorithmic": {
+                    "ops_per_update": FLOP_PER_UPDATE,
+                    "achieved": algorithmic_ops / 1e12,
+                    "unit": "T ops/s (each IEEE add, mul, compare, sqrt, div of the "
+                            "reference's update counted once)",
+                    "over_lane_instruction_peak": algorithmic_ops / peak_lane_ops,
+                    "note": "above 1 because the kernel runs fewer FP64 instructions than "
+                            "the reference's operation count: comparisons run on the integer "
+                            "pipe and operators of nodes that provably keep their value are "
+                            "skipped (exact, bitwise-tested)",
+                },
                 "kernel_ms": sweep,
                 "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
                         "frac": hbm_gbs / hbm_peak, "bytes_per_update": BYTES_PER_UPDATE},
                 "traffic": traffic,
-                "traffic_source": "ncu DRAM bytes per update on the 192-source 64x128x128 "
-                                  "case, scaled by updates per launch",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this "
+                                  "kernel on the 192-source 64x128x128 case, per node update, "
+                                  "times the updates of this launch",
             },
             "e2e": {
                 "value": e2e_shots,

@@ -18,6 +18,24 @@ from . import _device, _lib
 from ._solver import SPIN_LIMIT, solve3d_device
 
 
+def _velocity(velocity):
+    """The velocity model as a contiguous float64 tensor on the current CUDA
+    device (converted when it is not one already), detached from autograd."""
+    if not isinstance(velocity, torch.Tensor):
+        raise TypeError("velocity must be a torch.Tensor [nz, nx, ny]")
+    if velocity.dim() != 3:
+        raise ValueError("velocity must have shape [nz, nx, ny]")
+    return velocity.detach().to(device=_device.device(), dtype=torch.float64).contiguous()
+
+
+def _points(points, what):
+    """[n, 3] float64 host coordinates (a single point may be given as [3])."""
+    p = np.ascontiguousarray(np.atleast_2d(np.asarray(points, dtype=np.float64)))
+    if p.ndim != 2 or p.shape[-1] != 3 or len(p) == 0:
+        raise ValueError(f"{what} must have shape (3,) or (n, 3)")
+    return p
+
+
 def _node_axes(shape, gridsize):
     return [_device.to_device(gridsize[d] * np.arange(shape[d] + 1)) for d in range(3)]
 
@@ -44,9 +62,11 @@ class _Traveltimes(torch.autograd.Function):
     @staticmethod
     def forward(ctx, velocity, gridsize, sources, receivers, nsweep):
         lib = _lib.load()
-        slow = _device.slowness(velocity.detach().contiguous())
+        slow = _device.slowness(_velocity(velocity))
+        ctx.velocity_meta = (velocity.dtype, velocity.device)
         nz, nx, ny = slow.shape
-        src = np.ascontiguousarray(np.atleast_2d(sources), dtype=np.float64)
+        src = _points(sources, "sources")
+        receivers = _points(receivers, "receivers")
         nsrc = len(src)
         nsweep = max(int(nsweep), 0)
         dev = slow.device
@@ -95,7 +115,8 @@ class _Traveltimes(torch.autograd.Function):
         _lib.check(rc, "traveltimes backward")
         # slowness = 1 / velocity, so dL/dv = -dL/ds * s^2
         grad_velocity = -grad_slow * slow * slow
-        return grad_velocity, None, None, None, None
+        dtype, device = ctx.velocity_meta
+        return grad_velocity.to(device=device, dtype=dtype), None, None, None, None
 
 
 def traveltimes(velocity, gridsize, sources, receivers, nsweep=2):
@@ -104,10 +125,12 @@ def traveltimes(velocity, gridsize, sources, receivers, nsweep=2):
     Parameters
     ----------
     velocity : torch.Tensor
-        float64 CUDA tensor [nz, nx, ny] of cell velocities (``requires_grad``
-        to get d(loss)/d(velocity)).
+        [nz, nx, ny] cell velocities (``requires_grad`` to get
+        d(loss)/d(velocity)). The solve runs in float64 on the current CUDA
+        device; a tensor of another dtype or device is converted, and its
+        gradient comes back in its own dtype and device.
     gridsize : (dz, dx, dy)
-    sources, receivers : array_like [n, 3]
+    sources, receivers : array_like [n, 3] (or one point [3])
         Coordinates relative to the grid origin (node (0, 0, 0) at 0).
     nsweep : int
         Sweeps of the solve; the gradient is that of this many sweeps.
@@ -117,15 +140,15 @@ def traveltimes(velocity, gridsize, sources, receivers, nsweep=2):
     torch.Tensor [nsrc, nrec]: apparent-velocity interpolated traveltimes, the
     values ``TraveltimeGrid3D.__call__`` returns for an origin at 0.
     """
-    return _Traveltimes.apply(velocity, tuple(gridsize), np.asarray(sources, dtype=np.float64),
-                              np.asarray(receivers, dtype=np.float64), int(nsweep))
+    return _Traveltimes.apply(velocity, tuple(gridsize), _points(sources, "sources"),
+                              _points(receivers, "receivers"), int(nsweep))
 
 
 def converged(velocity, gridsize, sources, nsweep):
     """True when one more sweep would leave every traveltime unchanged, i.e.
     when the derivative of ``traveltimes`` is the derivative of the solve."""
-    slow = _device.slowness(velocity.detach().contiguous())
-    src = np.ascontiguousarray(sources, dtype=np.float64)
+    slow = _device.slowness(_velocity(velocity))
+    src = _points(sources, "sources")
     a, _, _ = solve3d_device(slow, gridsize, src, nsweep, False)
     a = a.clone()
     b, _, _ = solve3d_device(slow, gridsize, src, nsweep + 1, False)

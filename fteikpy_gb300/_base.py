@@ -56,6 +56,16 @@ class BaseGrid(ABC):
             self._axes_cache = [_device.to_device(a) for a in self._axes()]
         return self._axes_cache
 
+    @property
+    def tensor(self):
+        """The grid values as a float64 CUDA tensor: the device memory the
+        library computed them in (a solve's traveltimes, a batch's views), or
+        an upload of host values made once and cached. No copy is made for
+        device-resident values, so torch code can use a solve's result
+        directly. No counterpart in the reference, whose grids are NumPy
+        arrays (fteikpy/_base.py:22-25)."""
+        return self._device_grid()
+
     # -- reference API -----------------------------------------------------------
     def __getitem__(self, islice):
         """Slice grid."""

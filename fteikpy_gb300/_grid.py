@@ -38,6 +38,19 @@ class _TraveltimeMixin:
             self._gradient = g
         return g.contiguous()
 
+    @property
+    def gradient_tensor(self):
+        """The traveltime gradient, [..., ndim] float64 on the device: the
+        memory the solve wrote it to (no copy). No counterpart in the
+        reference, whose gradient grids are NumPy arrays (fteikpy/_grid.py:
+        148-158,268-278); raises the reference's error when the solve returned
+        no gradient."""
+        if self._gradient is None:
+            raise ValueError(
+                "no gradient grid, use option `return_gradient` to return gradient grids"
+            )
+        return self._device_gradient()
+
     def _device_source(self):
         """[source coordinates..., vzero] as a CUDA tensor, uploaded once (the
         per-call interpolation and ray tracing read them on the device)."""

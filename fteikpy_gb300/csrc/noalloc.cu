@@ -26,6 +26,11 @@
 //  * The first call on each device performs a one-time set-up on that device
 //    (it looks up the array's device address with cudaGetSymbolAddress while
 //    that device is current). Make that first call before any stream capture.
+//  * cudaDeviceReset (or anything else that replaces the device's primary
+//    context) reloads the library's device code, so the array may move. Every
+//    later call that is not made during a stream capture looks the address up
+//    again and keeps the new one; after a reset, make one call outside any
+//    capture before capturing calls again.
 #include <cstdio>
 #include <mutex>
 
@@ -44,14 +49,22 @@ constexpr int kMaxDevices = 64;
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (set up once per
-// device, with that device current).
-static int noalloc_scratch(void** out) {
+// Device address of the scratch array on the current device: looked up on the
+// device's first call, with that device current, and again on every call made
+// outside a stream capture (a device reset may have moved it). During a
+// capture the cached address is used.
+static int noalloc_scratch(void** out, cudaStream_t stream) {
   int dev = 0;
   FTEIK_CHECK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return kInvalidArgument;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  bool capturing = true;
+  if (cudaStreamIsCapturing(stream, &cs) == cudaSuccess)
+    capturing = cs != cudaStreamCaptureStatusNone;
+  else
+    (void)cudaGetLastError();  // an illegal query during another capture: treat as capturing
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || !capturing) {
     void* ptr = nullptr;
     FTEIK_CHECK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
     if (!ptr) return kCudaError;
@@ -78,7 +91,7 @@ extern "C" int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny,
     return kWorkspaceTooSmall;
   }
   void* scratch = nullptr;
-  const int rc0 = noalloc_scratch(&scratch);
+  const int rc0 = noalloc_scratch(&scratch, (cudaStream_t)stream);
   if (rc0 != kOk) return rc0;
   const int rc = fteik3d_solve_async(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, nsweep, grad,
                                      tt, ttgrad, vzero, scratch, FTEIK_NOALLOC_SCRATCH_BYTES,

@@ -180,7 +180,8 @@ const char* fteik_last_sweep_kernel(void);
  * share the array (it keeps the last call's contents; the solve clears what
  * must start at zero), so calls that overlap on the GPU race: serialise them.
  * The first call on each device does a one-time set-up with that device
- * current; make it before any stream capture. Blocking. */
+ * current; make it before any stream capture. A cudaDeviceReset may move the
+ * array: the next call made outside a stream capture finds it again. Blocking. */
 #define FTEIK_NOALLOC_SCRATCH_BYTES (64u << 20)
 int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny, double dz, double dx,
                           double dy, const double* sources, int nsrc, int nsweep, int grad,

@@ -18,8 +18,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfteik_oracle.so")
+# The same source compiled for timing only, with the floating-point licences
+# of the reference's numba build (fteikpy/_common.py:12: contract, arcp, nsz,
+# afn): the CPU baseline of the benchmark, never a parity checker.
+FAST_LIB_PATH = os.path.join(HERE, "_build", "libfteik_oracle_fast.so")
 
-_lib = None
+_libs = {}
 
 _D = ctypes.c_double
 _I = ctypes.c_int
@@ -32,14 +36,16 @@ def build():
     subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")])
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
-            os.path.join(HERE, "fteik_oracle.c")
-        ):
+def lib(fast=False):
+    """The bitwise oracle library, or with ``fast`` the timing build."""
+    path = FAST_LIB_PATH if fast else LIB_PATH
+    L = _libs.get(path)
+    if L is None:
+        src_time = max(os.path.getmtime(os.path.join(HERE, f))
+                       for f in ("fteik_oracle.c", "build_oracle.sh"))
+        if not os.path.exists(path) or os.path.getmtime(path) < src_time:
             build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(path)
         L.oracle_fteik3d_many.argtypes = [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _I]
         L.oracle_fteik3d_many.restype = _I
         L.oracle_fteik3d_record.argtypes = [_P, _I, _I, _I, _D, _D, _D, _D, _D, _D, _I, _P, _P, _P, _P]
@@ -54,8 +60,8 @@ def lib():
         L.oracle_vinterp2d.argtypes = [_P, _I, _P, _I, _P, _P, _I, _P, _D, _D, _P]
         L.oracle_ray3d.argtypes = [_P, _I, _P, _I, _P, _I, _P, _P, _I, _P, _D, _I, _I, _P, _P, _P]
         L.oracle_ray2d.argtypes = [_P, _I, _P, _I, _P, _P, _I, _P, _D, _I, _I, _P, _P, _P]
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return L
 
 
 def _c(a, dtype=np.float64):
@@ -66,8 +72,9 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-def solve3d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
+def solve3d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None, fast=False):
     """Batched 3D solve. ``sources`` is (nsrc, 3), relative to the grid origin.
+    ``fast`` runs the timing build (not bitwise).
 
     Returns (tt[nsrc, nz+1, nx+1, ny+1], ttgrad[nsrc, ..., 3] or None, vzero[nsrc]).
     """
@@ -79,7 +86,7 @@ def solve3d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
     tg = np.empty((nsrc, nz + 1, nx + 1, ny + 1, 3)) if grad else np.empty(1)
     vz = np.empty(nsrc)
     nthreads = nthreads or os.cpu_count()
-    st = lib().oracle_fteik3d_many(
+    st = lib(fast).oracle_fteik3d_many(
         _p(slow), nz, nx, ny, *map(float, gridsize), _p(src), nsrc, int(nsweep), int(grad),
         _p(tt), _p(tg), _p(vz), int(nthreads),
     )
@@ -126,7 +133,7 @@ def adjoint3d(slow, gridsize, sources, nsweep, receivers, grad_tt_rec, nthreads=
     return out
 
 
-def solve2d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
+def solve2d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None, fast=False):
     slow = _c(slow)
     src = _c(np.atleast_2d(sources))
     nz, nx = slow.shape
@@ -135,7 +142,7 @@ def solve2d(slow, gridsize, sources, nsweep=2, grad=False, nthreads=None):
     tg = np.empty((nsrc, nz + 1, nx + 1, 2)) if grad else np.empty(1)
     vz = np.empty(nsrc)
     nthreads = nthreads or os.cpu_count()
-    st = lib().oracle_fteik2d_many(
+    st = lib(fast).oracle_fteik2d_many(
         _p(slow), nz, nx, *map(float, gridsize), _p(src), nsrc, int(nsweep), int(grad),
         _p(tt), _p(tg), _p(vz), int(nthreads),
     )
@@ -189,7 +196,7 @@ def vinterp(ax, tt, points, source, vzero, fill_value=np.nan):
     return out
 
 
-def raytrace(ax, ttgrad, ends, source, stepsize, max_step, honor_grid=False):
+def raytrace(ax, ttgrad, ends, source, stepsize, max_step, honor_grid=False, fast=False):
     """Ray tracing (``_ray2d.py`` / ``_ray3d.py``). Returns a list of rays, each
     ordered source -> end point, as ``ray3d`` returns them."""
     nd = len(ax)
@@ -202,13 +209,13 @@ def raytrace(ax, ttgrad, ends, source, stepsize, max_step, honor_grid=False):
     counts = np.zeros(n, dtype=np.int32)
     status = np.zeros(n, dtype=np.int32)
     if nd == 3:
-        lib().oracle_ray3d(
+        lib(fast).oracle_ray3d(
             _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(ax[2]), len(ax[2]), _p(g),
             _p(ends), n, _p(src), float(stepsize), int(max_step), int(honor_grid), _p(rays),
             _p(counts), _p(status),
         )
     else:
-        lib().oracle_ray2d(
+        lib(fast).oracle_ray2d(
             _p(ax[0]), len(ax[0]), _p(ax[1]), len(ax[1]), _p(g), _p(ends), n, _p(src),
             float(stepsize), int(max_step), int(honor_grid), _p(rays), _p(counts), _p(status),
         )

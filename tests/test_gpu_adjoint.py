@@ -170,3 +170,21 @@ def test_reverse_pass_chunk_does_not_change_the_gradient():
     assert all(np.array_equal(grads[0], g) for g in grads[1:])
     go = oracle_velocity_gradient(v0, src, rec, nsweep, t_obs)
     assert np.abs(grads[0] - go).max() <= 1e-12 * np.abs(go).max()
+
+
+def test_float32_velocity_and_a_single_receiver_are_converted():
+    """A float32 velocity runs in float64 and gets its gradient back as
+    float32; one receiver may be given as [3]. Both equal the float64 call."""
+    shape, nsweep = (12, 14, 16), 2
+    src, rec = geometry(shape, 2, 5, 3)
+    v0 = velocity(shape, False, perturb=True).astype(np.float32).astype(np.float64)
+    v32 = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    T32 = fp.traveltimes(v32, D, src, rec[0], nsweep)
+    assert T32.shape == (len(src), 1) and T32.dtype == torch.float64
+    T32.sum().backward()
+    v64 = torch.tensor(v0, device="cuda", requires_grad=True)
+    T64 = fp.traveltimes(v64, D, src, rec[:1], nsweep)
+    T64.sum().backward()
+    assert torch.equal(T32, T64)
+    assert v32.grad.dtype == torch.float32
+    assert torch.equal(v32.grad, v64.grad.to(torch.float32))

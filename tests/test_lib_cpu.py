@@ -125,6 +125,27 @@ def test_api_host_logic():
     tt2 = fp.TraveltimeGrid2D(np.zeros((5, 6)), (1.0, 1.0), np.zeros(2), [0, 0], None, 1.0)
     with pytest.raises(ValueError, match="no gradient grid"):
         tt2.gradient
+    with pytest.raises(ValueError, match="no gradient grid"):
+        tt2.gradient_tensor
+
+
+def test_traveltimes_argument_checks_are_host_side():
+    """The differentiable traveltimes reject what the kernels could misread
+    before any device call: a velocity that is not a 3D tensor, and point
+    lists that are not [n, 3] (one point may be given as [3])."""
+    import torch
+
+    from fteikpy_gb300 import _adjoint
+
+    with pytest.raises(TypeError):
+        fp.traveltimes(np.ones((4, 5, 6)), (1.0, 1.0, 1.0), [[0, 1, 1]], [[0, 2, 2]])
+    with pytest.raises(ValueError, match="velocity must have shape"):
+        _adjoint._velocity(torch.ones((4, 5)))
+    with pytest.raises(ValueError, match="receivers must have shape"):
+        _adjoint._points([0.0, 1.0], "receivers")
+    with pytest.raises(ValueError, match="sources must have shape"):
+        _adjoint._points(np.zeros((2, 2)), "sources")
+    assert _adjoint._points([0.0, 1.0, 2.0], "receivers").shape == (1, 3)
 
 
 def test_grid_ops_host_checks(lib):

@@ -32,7 +32,7 @@ def _model(shape, seed):
     return v * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, shape))
 
 
-def _solve(lib, slow, d, src, nsweep, grad, noalloc):
+def _solve(lib, slow, d, src, nsweep, grad, noalloc, spin_limit=0, expect_ok=True):
     nz, nx, ny = slow.shape
     n = len(src)
     dev = slow.device
@@ -43,11 +43,13 @@ def _solve(lib, slow, d, src, nsweep, grad, noalloc):
     args = (_device.ptr(slow), nz, nx, ny, *d, srch.ctypes.data_as(ctypes.c_void_p), n, nsweep,
             int(grad), _device.ptr(tt), _device.ptr(tg), _device.ptr(vz))
     if noalloc:
-        rc = lib.fteik3d_solve_noalloc(*args, 0, _device.stream())
+        rc = lib.fteik3d_solve_noalloc(*args, spin_limit, _device.stream())
     else:
         ws = torch.empty(lib.fteik3d_workspace_bytes(nz, nx, ny, n, int(grad)), dtype=torch.uint8,
                          device=dev)
-        rc = lib.fteik3d_solve(*args, _device.ptr(ws), ws.numel(), 0, _device.stream())
+        rc = lib.fteik3d_solve(*args, _device.ptr(ws), ws.numel(), spin_limit, _device.stream())
+    if not expect_ok:
+        return rc
     assert rc == _lib.OK, (rc, lib.fteik_last_error())
     return tt.cpu().numpy(), (tg.cpu().numpy() if grad else None), vz.cpu().numpy()
 
@@ -73,6 +75,34 @@ def test_noalloc_solve_matches_workspace_solve_twice():
         if grad:
             assert np.array_equal(a[1], b[1])
         assert np.array_equal(a[2], b[2])
+
+
+def test_noalloc_team_kernel_after_a_timed_out_call():
+    """The shared array after a call that gave up: a call whose device-side
+    waits are limited to one poll (which may time out and leave a non-zero
+    status and half-advanced counters in the array), then a regular call with
+    blocks of several sources stepping together (6 sources, not a multiple of
+    the block's 4), which must equal the workspace solve bit for bit."""
+    lib = _lib.load()
+    torch.cuda.set_device(0)
+    shape, d = (20, 28, 36), (10.0, 10.0, 10.0)
+    rng = np.random.default_rng(8)
+    src = np.column_stack([rng.uniform(0, 200, 6), rng.uniform(0, 280, 6), rng.uniform(0, 360, 6)])
+    slow = _device.slowness(_device.to_device(_model(shape, 4)))
+    rc = _solve(lib, slow, d, src, 2, True, noalloc=True, spin_limit=1, expect_ok=False)
+    assert rc in (_lib.OK, _lib.DEVICE_WAIT_TIMEOUT), (rc, lib.fteik_last_error())
+    assert lib.fteik_set_option(b"sweep_team", 1) == _lib.OK
+    try:
+        for _ in range(2):
+            a = _solve(lib, slow, d, src, 2, True, noalloc=True)
+            assert lib.fteik_last_sweep_kernel() == b"sweep3d_team_kernel"
+            b = _solve(lib, slow, d, src, 2, True, noalloc=False)
+            assert _rel(a[0], b[0]) <= TOL
+            assert np.array_equal(a[0], b[0])
+            assert np.array_equal(a[1], b[1])
+            assert np.array_equal(a[2], b[2])
+    finally:
+        lib.fteik_set_option(b"sweep_team", -1)
 
 
 def test_noalloc_rejects_problems_above_the_fixed_scratch():

@@ -552,33 +552,118 @@ def tomography_models(shape=(96, 128, 128), d=D, seed=5):
     return v0, v0 * (1.0 + 0.08 * np.exp(-r2 / (2.0 * 150.0**2)))
 
 
+def tie_broken(v, rel=1e-3, seed=17):
+    """``v`` with every cell's velocity times (1 + rel u), u seeded uniform in
+    [-1, 1]: on a linear-gradient model this breaks the exact ties between
+    laterally neighbouring cells that the solver's slowness minima take."""
+    return v * (1.0 + rel * np.random.default_rng(seed).uniform(-1.0, 1.0, v.shape))
+
+
+def oracle_receiver_times(O, v, src, rec, nsweep=NSWEEP, probe=False, margin=0.0):
+    """[nsrc, nrec] apparent-velocity traveltimes through the oracle; with
+    ``probe`` also the per-source decision digests and the near-tied cells."""
+    if probe:
+        tt, vz, dig, tied = O.solve3d_probe(1.0 / v, D, src, nsweep, margin=margin)
+    else:
+        tt, _, vz = O.solve3d(1.0 / v, D, src, nsweep, False)
+        dig = tied = None
+    ax = O.axes(tt.shape[1:], D, np.zeros(3))
+    T = np.stack([O.vinterp(ax, tt[s], rec, src[s], vz[s]) for s in range(len(src))])
+    return T, dig, tied
+
+
+FD_STEP = 1e-6    # relative step of the central differences
+TIE_MARGIN = 4e-6  # relative margin a slowness minimum needs to count as untied
+
+
+def fd_check(O, v, src, rec, t_obs, g, ncells, tie_free, min_frac, seed=3):
+    """Central differences (relative step 1e-6) of 0.5 sum (T - t_obs)^2 through
+    the oracle's solve, against the gradient ``g``, on seeded cells whose
+    |g| is at least ``min_frac`` of the largest.
+
+    With ``tie_free`` a cell qualifies only away from the solver's branch
+    ties: no slowness minimum taken by a kept operator may have another cell
+    within TIE_MARGIN of it (oracle probe at ``v``), and every decision of
+    the sweeps (candidate kept, cells attaining each minimum) must be the same
+    at v + h and v - h as at v (oracle decision digests); candidates that
+    fail are skipped and counted. Returns a dict of the statistics."""
+    shape = v.shape
+    gmax = float(np.abs(g).max())
+    _, dig0, tied = oracle_receiver_times(O, v, src, rec, probe=True, margin=TIE_MARGIN)
+    pool = np.flatnonzero(np.abs(g.ravel()) >= min_frac * gmax)
+    significant = len(pool)
+    if tie_free:
+        pool = pool[~tied.ravel()[pool]]
+    order = np.random.default_rng(seed).permutation(pool)
+    errs, rejected = [], 0
+    for c in order:
+        if len(errs) >= ncells:
+            break
+        idx = np.unravel_index(c, shape)
+        h = FD_STEP * v[idx]
+        vp = v.copy()
+        vp[idx] += h
+        vm = v.copy()
+        vm[idx] -= h
+        tp, dp, _ = oracle_receiver_times(O, vp, src, rec, probe=tie_free, margin=TIE_MARGIN)
+        tm, dm, _ = oracle_receiver_times(O, vm, src, rec, probe=tie_free, margin=TIE_MARGIN)
+        if tie_free and not (np.array_equal(dp, dig0) and np.array_equal(dm, dig0)):
+            rejected += 1
+            continue
+        # L(v+h) - L(v-h) summed term by term as 0.5 (tp - tm)(tp + tm - 2 t_obs):
+        # the same difference without cancelling two losses ~1e8 times larger
+        fd = float(np.sum(0.5 * (tp - tm) * (tp + tm - 2.0 * t_obs))) / (2.0 * h)
+        errs.append(abs(fd - g[idx]) / abs(fd))
+    errs = np.array(errs)
+    return {
+        "cells": int(len(errs)),
+        "significant_cells": int(significant),
+        "eligible_cells": int(len(pool)),
+        "rejected_decision_change": int(rejected) if tie_free else None,
+        "min_abs_grad_over_max": min_frac,
+        "rel_err_median": float(np.median(errs)) if len(errs) else None,
+        "rel_err_p90": float(np.quantile(errs, 0.9)) if len(errs) else None,
+        "rel_err_max": float(errs.max()) if len(errs) else None,
+        "cells_within_1e-6": int((errs <= 1e-6).sum()),
+        "cells_within_1e-4": int((errs <= 1e-4).sum()),
+    }
+
+
 def run_config5(args):
     """Adjoint gradient for tomography: 96 x 128 x 128 at 10 m, 64 surface
     sources x 400 surface receivers, loss = 0.5 sum((T_pred - T_obs)^2) with
     T_obs from the true model; forward and adjoint through the autograd
     function, the gradient checked by central differences (relative step 1e-6)
-    on 50 seeded cells through the C oracle."""
+    on 50 seeded cells through the C oracle: on cells away from the solver's
+    branch ties of the start model with its lateral ties broken, and on
+    |grad|-selected cells of the exact start model."""
     import torch
 
     import fteikpy_gb300 as fp
+    from fteikpy_gb300 import _adjoint, _lib
     from fteikpy_gb300._solver import solve3d_device
     from oracle import oracle as O
 
-    shape = (48, 64, 64) if args.small else (96, 128, 128)
+    if args.adj_shape:
+        shape = tuple(int(x) for x in args.adj_shape.split(","))
+    else:
+        shape = (48, 64, 64) if args.small else (96, 128, 128)
+    n_side = int(round(np.sqrt(args.adj_sources))) if args.adj_sources else (4 if args.small else 8)
     v0, vt = tomography_models(shape)
-    src = surface_sources(shape, n_side=4 if args.small else 8, seed=7)
+    src = surface_sources(shape, n_side=n_side, seed=7)
     rec = surface_receivers(shape, n=NREC, seed=11)
     dev = torch.device("cuda", 0)
-    t_obs = fp.traveltimes(torch.tensor(vt, device=dev), D, src, rec, NSWEEP).detach()
+    budget = int(args.memory_budget * 1e9) if args.memory_budget else None
+    t_obs = fp.traveltimes(torch.tensor(vt, device=dev), D, src, rec, NSWEEP, budget).detach()
     vel = torch.tensor(v0, device=dev)
 
     def fwd_plain():
         slow = 1.0 / vel
         return solve3d_device(slow, D, src, NSWEEP, False)[0]
 
-    def step():
-        x = vel.clone().requires_grad_(True)
-        T = fp.traveltimes(x, D, src, rec, NSWEEP)
+    def step(v=vel):
+        x = v.clone().requires_grad_(True)
+        T = fp.traveltimes(x, D, src, rec, NSWEEP, budget)
         loss = 0.5 * ((T - t_obs) ** 2).sum()
         e_mid.record()
         loss.backward()
@@ -589,6 +674,8 @@ def run_config5(args):
         fwd_plain()
         step()
     torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(dev)
+    base_mem = torch.cuda.memory_allocated(dev)
     plain_ms, fwd_ms, bwd_ms = [], [], []
     for _ in range(max(args.steps, 1)):
         e0.record()
@@ -602,71 +689,70 @@ def run_config5(args):
         torch.cuda.synchronize()
         fwd_ms.append(e0.elapsed_time(e_mid))
         bwd_ms.append(e_mid.elapsed_time(e1))
+    peak_mem = torch.cuda.max_memory_allocated(dev) - base_mem
+    lib = _lib.load()
+    used_budget = budget if budget is not None else int(
+        _adjoint.BUDGET_SHARE * torch.cuda.mem_get_info(dev)[0])
+    chunk, _ = _adjoint._chunk_plan(lib, shape, len(src), NSWEEP, used_budget)
     g = g.cpu().numpy()
     T = T.detach().cpu().numpy()
     t_obs_h = t_obs.cpu().numpy()
     plain, fwd, bwd = (float(np.median(x)) for x in (plain_ms, fwd_ms, bwd_ms))
-
-    def oracle_times(v):
-        tt, _, vz = O.solve3d(1.0 / v, D, src, NSWEEP, False)
-        ax = O.axes(tt.shape[1:], D, np.zeros(3))
-        return np.stack([O.vinterp(ax, tt[s], rec, src[s], vz[s]) for s in range(len(src))])
-
-    # CPU: the oracle's forward and its sequential reverse-mode adjoint, which
-    # the GPU gradient must equal on every cell
-    q0 = time.perf_counter()
-    t_oracle = oracle_times(v0)
-    cpu_fwd = time.perf_counter() - q0
-    q0 = time.perf_counter()
-    s0 = 1.0 / v0
-    g_oracle = -O.adjoint3d(s0, D, src, NSWEEP, rec, t_oracle - t_obs_h) * s0 * s0
-    cpu_adj = time.perf_counter() - q0
-    gmax = float(np.abs(g).max())
-    # central differences (relative step 1e-6) through the oracle's solve on
-    # seeded cells whose derivative is at least 1e-4 of the largest (smaller
-    # ones drown in the rounding of the differences)
-    rng = np.random.default_rng(3)
-    pool = np.flatnonzero(np.abs(g.ravel()) >= 1e-4 * gmax)
-    cells = rng.choice(pool, min(args.fd_cells, len(pool)), replace=False)
-    rows, fds = [], []
-    for c in cells:
-        idx = np.unravel_index(c, shape)
-        h = 1e-6 * v0[idx]
-        vp = v0.copy()
-        vp[idx] += h
-        vm = v0.copy()
-        vm[idx] -= h
-        tp, tm = oracle_times(vp), oracle_times(vm)
-        # L(v+h) - L(v-h) summed term by term as 0.5 (tp - tm)(tp + tm - 2 t_obs):
-        # the same difference without cancelling two losses ~1e8 times larger
-        fd = float(np.sum(0.5 * (tp - tm) * (tp + tm - 2.0 * t_obs_h))) / (2.0 * h)
-        fds.append(fd)
-        rows.append(abs(fd - g[idx]) / abs(fd))
-    rows = np.array(rows)
-    if args.dump:
-        np.savez_compressed(args.dump, grad=g, grad_oracle=g_oracle, cells=cells, fd=np.array(fds),
-                            v0=v0, t_obs=t_obs_h, t_pred=T)
-    print(json.dumps({
+    line = {
         "config": 5,
         "metric": "adjoint d(loss)/d(velocity), %dx%dx%d, %d sources x 400 receivers, nsweep=2"
                   % (shape + (len(src),)),
         "value": fwd + bwd, "unit": "ms", "higher_is_better": False,
         "forward_plain_ms": plain, "forward_with_tape_ms": fwd, "adjoint_ms": bwd,
         "adjoint_over_forward": bwd / plain, "forward_plus_adjoint_over_forward": (fwd + bwd) / plain,
-        "forward_bitwise_vs_oracle": bool(np.array_equal(T, t_oracle)),
-        "adjoint_vs_oracle_adjoint_max_abs_over_gmax": float(np.abs(g - g_oracle).max() / gmax),
-        "fd": {"cells": int(len(cells)), "rel_step": 1e-6,
-               "selection": "seeded, |grad| >= 1e-4 max|grad|",
-               "rel_err_median": float(np.median(rows)) if len(rows) else None,
-               "rel_err_p90": float(np.quantile(rows, 0.9)) if len(rows) else None,
-               "rel_err_max": float(rows.max()) if len(rows) else None,
-               "cells_within_1e-6": int((rows <= 1e-6).sum()),
-               "cells_within_1e-4": int((rows <= 1e-4).sum())},
-        "cpu_baseline": {"value": 1e3 * (cpu_fwd + cpu_adj), "unit": "ms",
-                         "cores": os.cpu_count(), "kind": "port",
-                         "sample": "one forward + adjoint with the C oracle (OpenMP over sources)",
-                         "forward_ms": 1e3 * cpu_fwd, "adjoint_ms": 1e3 * cpu_adj},
-    }))
+        "memory": {"peak_bytes_above_inputs": int(peak_mem), "budget_bytes": used_budget,
+                   "sources_per_chunk": chunk,
+                   "tape_bytes_per_node_source": lib.fteik3d_tape_bytes(*shape, 1, NSWEEP, 2)
+                   / float(np.prod(np.array(shape) + 1))},
+    }
+    if not args.no_cpu:
+        # CPU: the oracle's forward and its sequential reverse-mode adjoint,
+        # which the GPU gradient must equal on every cell
+        q0 = time.perf_counter()
+        t_oracle = oracle_receiver_times(O, v0, src, rec)[0]
+        cpu_fwd = time.perf_counter() - q0
+        q0 = time.perf_counter()
+        s0 = 1.0 / v0
+        g_oracle = -O.adjoint3d(s0, D, src, NSWEEP, rec, t_oracle - t_obs_h) * s0 * s0
+        cpu_adj = time.perf_counter() - q0
+        gmax = float(np.abs(g).max())
+        line["forward_bitwise_vs_oracle"] = bool(np.array_equal(T, t_oracle))
+        line["adjoint_vs_oracle_adjoint_max_abs_over_gmax"] = float(np.abs(g - g_oracle).max() / gmax)
+        line["cpu_baseline"] = {"value": 1e3 * (cpu_fwd + cpu_adj), "unit": "ms",
+                                "cores": os.cpu_count(), "kind": "port",
+                                "sample": "one forward + adjoint with the C oracle "
+                                          "(OpenMP over sources)",
+                                "forward_ms": 1e3 * cpu_fwd, "adjoint_ms": 1e3 * cpu_adj}
+    if args.fd_cells > 0:
+        # 1. away from branch ties: the start model with its lateral ties
+        #    broken (each cell within 0.1%), cells whose slowness minima are
+        #    untied and whose sweeps decide alike at v +- h; derivatives of at
+        #    least 1% of the largest (below that the rounding of the
+        #    traveltimes, about 4e-10 of the largest derivative in the
+        #    central difference, passes 1e-6 of the cell's own)
+        vb = tie_broken(v0)
+        gb = step(torch.tensor(vb, device=dev))[0].cpu().numpy()
+        tie_free = fd_check(O, vb, src, rec, t_obs_h, gb, args.fd_cells, True, 1e-2)
+        tie_free["model"] = ("the start model with every cell's velocity times (1 + 1e-3 u), u "
+                             "seeded uniform in [-1, 1]")
+        tie_free["selection"] = ("seeded; |grad| >= 1e-2 max|grad|; no kept operator's slowness "
+                                 "minimum has a second cell within 4e-6 of it; the sweeps' "
+                                 "decisions (oracle digests) identical at v - h, v, v + h")
+        # 2. the exact start model: how many significant cells are tie-free,
+        #    and the |grad|-selected cells, ties included
+        start = fd_check(O, v0, src, rec, t_obs_h, g, args.fd_cells, False, 1e-4)
+        _, _, tied0 = oracle_receiver_times(O, v0, src, rec, probe=True, margin=TIE_MARGIN)
+        pool0 = np.flatnonzero(np.abs(g.ravel()) >= 1e-4 * np.abs(g).max())
+        start["tie_free_significant_cells"] = int((~tied0.ravel()[pool0]).sum())
+        start["selection"] = "seeded, |grad| >= 1e-4 max|grad| (ties included)"
+        line["fd"] = {"rel_step": FD_STEP, "cells_within_1e-6": tie_free["cells_within_1e-6"],
+                      "tie_free": tie_free, "start_model": start}
+    print(json.dumps(line))
     return 0
 
 
@@ -687,8 +773,13 @@ def main():
                          "(default), 4: uneven multi-model batch, 5: adjoint gradient")
     ap.add_argument("--fd-cells", type=int, default=50,
                     help="cells of the finite-difference check of --config 5")
-    ap.add_argument("--dump", default=None,
-                    help="--config 5: save the gradient and the finite differences (.npz)")
+    ap.add_argument("--adj-shape", default=None,
+                    help="--config 5: grid cells nz,nx,ny (default 96,128,128)")
+    ap.add_argument("--adj-sources", type=int, default=0,
+                    help="--config 5: sources on a square surface grid (default 64)")
+    ap.add_argument("--memory-budget", type=float, default=0.0,
+                    help="--config 5: device GB the tapes and workspaces may take "
+                         "(default: 80%% of the free memory)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: 192 sources on a 64x128x128 grid (1.7 GB of traveltimes, "
                          "> L2; 108K items per sweep, so the same team kernel as the full step); "

@@ -6,9 +6,11 @@ of the GPU path. The forward pass is the reference's solve
 (``fteikpy/_fteik/_fteik3d.py``) followed by its apparent-velocity
 interpolation at the receivers (``fteikpy/_interp/_vinterp3d.py``); the
 backward pass maps d(loss)/d(receiver traveltimes) to d(loss)/d(velocity).
-The forward solve keeps a tape of every sweep (``fteik3d_solve_tape``), and the
-backward pass is the exact reverse-mode derivative of those sweeps, so it
-matches finite differences of the solver for any ``nsweep``.
+The forward solve keeps a tape of every change its sweeps make
+(``fteik3d_solve_tape``), and the backward pass is the exact reverse-mode
+derivative of those sweeps, so it matches finite differences of the solver for
+any ``nsweep``. Sources run in chunks sized to a device-memory budget; a chunk
+whose tape is not kept is solved again in the backward pass.
 """
 
 import numpy as np
@@ -58,9 +60,67 @@ def _receiver_times(tt, axes, src_dev, vzero, receivers):
     return out.view(nsrc, nrec)
 
 
+# History slots of the tape per node: the values replaced by a node's 2nd and
+# 3rd changes (its later changes go to the tape's overflow table). A solve
+# whose table overflows is run again with more slots.
+HISTORY = 2
+# Share of the free device memory one differentiable solve may take for its
+# tapes and workspaces when no budget is given.
+BUDGET_SHARE = 0.8
+
+
+def _history_steps(nsweep):
+    """The history slot counts to try in turn: 2, 6, then every sweep's."""
+    top = max(8 * nsweep - 1, 0)
+    steps = [h for h in (HISTORY, 6) if h < top]
+    return steps + [top]
+
+
+def _taped_solve(lib, slow, gridsize, src, nsweep, history, workspace):
+    """fteik3d_solve_tape for the sources ``src`` (host [k, 3]); retries with
+    more history slots while the tape's overflow table is too small. Returns
+    (tt, vzero, tape, history)."""
+    nz, nx, ny = slow.shape
+    k = len(src)
+    dev = slow.device
+    tt = torch.empty((k, nz + 1, nx + 1, ny + 1), dtype=torch.float64, device=dev)
+    vzero = torch.empty(k, dtype=torch.float64, device=dev)
+    steps = [history] if history is not None else _history_steps(nsweep)
+    for h in steps:
+        tape = torch.empty(lib.fteik3d_tape_bytes(nz, nx, ny, k, nsweep, h), dtype=torch.uint8,
+                           device=dev)
+        rc = lib.fteik3d_solve_tape(
+            _device.ptr(slow), nz, nx, ny, *gridsize, _device.host_ptr(src), k, nsweep,
+            _device.ptr(tt), _device.ptr(vzero), _device.ptr(workspace), workspace.numel(), h,
+            _device.ptr(tape), tape.numel(), SPIN_LIMIT, _device.stream(),
+        )
+        if rc != _lib.TAPE_OVERFLOW:
+            _lib.check(rc, "traveltimes")
+            return tt, vzero, tape, h
+        del tape
+    _lib.check(rc, "traveltimes")
+
+
+def _chunk_plan(lib, shape, nsrc, nsweep, budget):
+    """Sources per chunk, so that one chunk's traveltimes, tape, solve and
+    adjoint workspaces fit ``budget`` bytes (at least one source)."""
+    nz, nx, ny = shape
+
+    def need(k):
+        nodes = (nz + 1) * (nx + 1) * (ny + 1)
+        return (8 * nodes * k + lib.fteik3d_workspace_bytes(nz, nx, ny, k, 2)
+                + lib.fteik3d_tape_bytes(nz, nx, ny, k, nsweep, min(HISTORY, max(8 * nsweep - 1, 0)))
+                + lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, k))
+
+    k = nsrc
+    while k > 1 and need(k) > budget:
+        k = (k + 1) // 2
+    return k, need(k)
+
+
 class _Traveltimes(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, velocity, gridsize, sources, receivers, nsweep):
+    def forward(ctx, velocity, gridsize, sources, receivers, nsweep, budget):
         lib = _lib.load()
         slow = _device.slowness(_velocity(velocity))
         ctx.velocity_meta = (velocity.dtype, velocity.device)
@@ -69,57 +129,76 @@ class _Traveltimes(torch.autograd.Function):
         receivers = _points(receivers, "receivers")
         nsrc = len(src)
         nsweep = max(int(nsweep), 0)
+        gs = tuple(float(g) for g in gridsize)
         dev = slow.device
-        ws = torch.empty(lib.fteik3d_workspace_bytes(nz, nx, ny, nsrc, 2), dtype=torch.uint8,
-                         device=dev)
-        tape = torch.empty(lib.fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep), dtype=torch.uint8,
-                           device=dev)
-        tt = torch.empty((nsrc, nz + 1, nx + 1, ny + 1), dtype=torch.float64, device=dev)
-        vzero = torch.empty(nsrc, dtype=torch.float64, device=dev)
-        rc = lib.fteik3d_solve_tape(
-            _device.ptr(slow), nz, nx, ny, *[float(g) for g in gridsize], _device.host_ptr(src),
-            nsrc, nsweep, _device.ptr(tt), _device.ptr(vzero), _device.ptr(ws), ws.numel(),
-            _device.ptr(tape), tape.numel(), SPIN_LIMIT, _device.stream(),
-        )
-        _lib.check(rc, "traveltimes")
-        axes = _node_axes(slow.shape, gridsize)
+        if budget is None:
+            budget = int(BUDGET_SHARE * torch.cuda.mem_get_info(dev)[0])
+        k, chunk_bytes = _chunk_plan(lib, slow.shape, nsrc, nsweep, int(budget))
+        axes = _node_axes(slow.shape, gs)
         src_dev = _device.to_device(src)
-        rec = _device.to_device(np.ascontiguousarray(receivers, dtype=np.float64))
-        times = _receiver_times(tt, axes, src_dev, vzero, rec)
-        ctx.save_for_backward(slow, tt, ws, tape, src_dev, rec)
+        rec = _device.to_device(receivers)
+        times = torch.empty((nsrc, len(receivers)), dtype=torch.float64, device=dev)
+        ws = torch.empty(lib.fteik3d_workspace_bytes(nz, nx, ny, k, 2), dtype=torch.uint8,
+                         device=dev)
+        # Keep each chunk's traveltimes and tape for the backward pass while
+        # they fit beside the working set of one more chunk; the backward pass
+        # solves the others again.
+        kept_bytes, chunks = 0, []
+        for a in range(0, nsrc, k):
+            b = min(a + k, nsrc)
+            tt, vzero, tape, h = _taped_solve(lib, slow, gs, src[a:b], nsweep, None, ws)
+            times[a:b] = _receiver_times(tt, axes, src_dev[a:b], vzero, rec)
+            size = tt.numel() * 8 + tape.numel()
+            if kept_bytes + size + chunk_bytes <= budget:
+                kept_bytes += size
+                chunks.append((a, b, h, tt, tape))
+            else:
+                chunks.append((a, b, h, None, None))
+            del tt, tape
+        ctx.save_for_backward(slow, src_dev, rec)
+        ctx.src = src
+        ctx.chunks = chunks
         ctx.nsweep = nsweep
-        ctx.gridsize = tuple(float(g) for g in gridsize)
+        ctx.gridsize = gs
         ctx.axes = axes
         return times
 
     @staticmethod
     def backward(ctx, grad_times):
         lib = _lib.load()
-        slow, tt, ws, tape, src_dev, rec = ctx.saved_tensors
+        slow, src_dev, rec = ctx.saved_tensors
         nz, nx, ny = slow.shape
-        nsrc = tt.shape[0]
         g = grad_times.detach().to(torch.float64).contiguous()
         grad_slow = torch.empty_like(slow)
-        aws = torch.empty(
-            lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, nsrc), dtype=torch.uint8,
-            device=slow.device,
-        )
         ax = ctx.axes
-        rc = lib.fteik3d_adjoint(
-            _device.ptr(slow), nz, nx, ny, *ctx.gridsize, nsrc, ctx.nsweep, _device.ptr(tt),
-            _device.ptr(ws), ws.numel(), _device.ptr(tape), tape.numel(), _device.ptr(ax[0]),
-            _device.ptr(ax[1]), _device.ptr(ax[2]),
-            _device.ptr(src_dev), _device.ptr(rec), rec.shape[0], _device.ptr(g),
-            _device.ptr(grad_slow), _device.ptr(aws), aws.numel(), SPIN_LIMIT, _device.stream(),
-        )
-        _lib.check(rc, "traveltimes backward")
+        ws = None
+        for c, (a, b, h, tt, tape) in enumerate(ctx.chunks):
+            k = b - a
+            if tt is None:  # not kept: solve this chunk again (same tape, same bits)
+                if ws is None:
+                    ws = torch.empty(lib.fteik3d_workspace_bytes(nz, nx, ny, k, 2),
+                                     dtype=torch.uint8, device=slow.device)
+                tt, _, tape, _ = _taped_solve(lib, slow, ctx.gridsize, ctx.src[a:b], ctx.nsweep,
+                                              h, ws)
+            aws = torch.empty(lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, k),
+                              dtype=torch.uint8, device=slow.device)
+            rc = lib.fteik3d_adjoint(
+                _device.ptr(slow), nz, nx, ny, *ctx.gridsize, k, ctx.nsweep, _device.ptr(tt), h,
+                _device.ptr(tape), tape.numel(), _device.ptr(ax[0]), _device.ptr(ax[1]),
+                _device.ptr(ax[2]), _device.ptr(src_dev[a:b]), _device.ptr(rec), rec.shape[0],
+                _device.ptr(g[a:b]), int(c > 0), _device.ptr(grad_slow), _device.ptr(aws),
+                aws.numel(), SPIN_LIMIT, _device.stream(),
+            )
+            _lib.check(rc, "traveltimes backward")
+            del tt, tape, aws
+        ctx.chunks = None
         # slowness = 1 / velocity, so dL/dv = -dL/ds * s^2
         grad_velocity = -grad_slow * slow * slow
         dtype, device = ctx.velocity_meta
-        return grad_velocity.to(device=device, dtype=dtype), None, None, None, None
+        return grad_velocity.to(device=device, dtype=dtype), None, None, None, None, None
 
 
-def traveltimes(velocity, gridsize, sources, receivers, nsweep=2):
+def traveltimes(velocity, gridsize, sources, receivers, nsweep=2, memory_budget=None):
     """Traveltimes from every source to every receiver, differentiable in velocity.
 
     Parameters
@@ -134,6 +213,12 @@ def traveltimes(velocity, gridsize, sources, receivers, nsweep=2):
         Coordinates relative to the grid origin (node (0, 0, 0) at 0).
     nsweep : int
         Sweeps of the solve; the gradient is that of this many sweeps.
+    memory_budget : int or None
+        Device bytes the solve's tapes and workspaces may take (default: 80%
+        of the free device memory). Sources are solved in consecutive chunks
+        that fit it; the tapes of the chunks that do not fit beside the
+        others are dropped after the forward pass and solved again in the
+        backward pass. The gradient's bits do not depend on the chunking.
 
     Returns
     -------
@@ -141,7 +226,7 @@ def traveltimes(velocity, gridsize, sources, receivers, nsweep=2):
     values ``TraveltimeGrid3D.__call__`` returns for an origin at 0.
     """
     return _Traveltimes.apply(velocity, tuple(gridsize), _points(sources, "sources"),
-                              _points(receivers, "receivers"), int(nsweep))
+                              _points(receivers, "receivers"), int(nsweep), memory_budget)
 
 
 def converged(velocity, gridsize, sources, nsweep):

@@ -47,13 +47,13 @@ SIGNATURES = {
     ),
     "fteik_clear_tuning": (_I, []),
     "fteik_last_sweep_kernel": (ctypes.c_char_p, []),
-    "fteik3d_tape_bytes": (_SZ, [_I, _I, _I, _I, _I]),
+    "fteik3d_tape_bytes": (_SZ, [_I, _I, _I, _I, _I, _I]),
     "fteik3d_solve_tape": (
-        _I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _P, _P, _SZ, _P, _SZ, _LL, _P]
+        _I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _P, _P, _SZ, _I, _P, _SZ, _LL, _P]
     ),
     "fteik3d_adjoint": (
         _I,
-        [_P, _I, _I, _I, _D, _D, _D, _I, _I, _P, _P, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _I, _P,
+        [_P, _I, _I, _I, _D, _D, _D, _I, _I, _P, _I, _P, _SZ, _P, _P, _P, _P, _P, _I, _P, _I,
          _P, _P, _SZ, _LL, _P],
     ),
     "fteik_resample": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
@@ -77,6 +77,7 @@ DEVICE_WAIT_TIMEOUT = 4
 INVALID_ARGUMENT = 5
 CUDA_ERROR = 6
 WORKSPACE_TOO_SMALL = 7
+TAPE_OVERFLOW = 8
 
 _lock = threading.Lock()
 _lib = None
@@ -121,5 +122,7 @@ def check(rc, what=""):
         raise ValueError(f"{what}: invalid argument")
     if rc == WORKSPACE_TOO_SMALL:
         raise RuntimeError(f"{what}: workspace too small")
+    if rc == TAPE_OVERFLOW:
+        raise RuntimeError(f"{what}: the adjoint's tape overflowed")
     err = load().fteik_last_error().decode()
     raise RuntimeError(f"{what}: CUDA error {err}")

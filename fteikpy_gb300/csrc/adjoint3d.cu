@@ -38,8 +38,7 @@ struct RevArgs {
   double* lam;           // [nsrc][nodes] adjoint of each node's current value
   double* contrib;       // [nsrc][nodes][7] adjoint a changed node sends to each input
   double* g8;            // [nsrc][nodes][8] dL/ds per node, by surrounding cell
-  const uint8_t* tcode;  // [nepochs][nsrc][nodes] operator code of each change (255: none)
-  const double* told;    // [nepochs][nsrc][nodes] value each change replaced
+  Tape3 tape;            // the forward's record of every change (see Tape3)
   int nz, nx, ny, NZ, NX, NY;
   long long nodes;
   int nsrc;
@@ -274,6 +273,34 @@ __device__ __forceinline__ void pencil_at(int p, int PJ, int PK, int& JL, int& K
   }
 }
 
+// The value that the change of node n = (i, j, k) of source src in sweep e
+// replaced (see Tape3): its initial value for a first change (Big, or the
+// analytic value kept for the 8 nodes around the source), else the history
+// slot or the overflow table.  Flags FTEIK_TAPE_OVERFLOW if the table lacks
+// the entry (which a solve that reported no overflow never leaves).
+__device__ __forceinline__ double tape_replaced(const Tape3& P, int src, long long sn,
+                                                const uint8_t* rec, int e, int i, int j, int k,
+                                                int zsi, int xsi, int ysi, int* status) {
+  const int m = tape_changes_before(rec, e) + 1;
+  if (m == 1) {
+    const int a = i - zsi, b = j - xsi, c = k - ysi;
+    if ((unsigned)a <= 1u && (unsigned)b <= 1u && (unsigned)c <= 1u)
+      return __ldg(P.init8 + src * 8 + a + 2 * b + 4 * c);
+    return kBig;
+  }
+  if (m - 2 < P.H) return __ldg(P.hist + sn * P.H + (m - 2));
+  const unsigned long long key = tape_key(sn, m);
+  unsigned long long h = tape_slot(key, P.mask);
+  for (int q = 0; q < kTapeProbes; ++q) {
+    const unsigned long long kq = __ldg(P.key + h);
+    if (kq == key) return __ldg(P.val + h);
+    if (kq == 0ull) break;
+    h = (h + 1) & P.mask;
+  }
+  atomicCAS(status, 0, (int)kTapeOverflow);
+  return kBig;
+}
+
 // Whether the operator with signs (az, ax, ay) reads input slot (bz, bx, by).
 __device__ __forceinline__ bool uses_slot(int az, int ax, int ay, int bz, int bx, int by) {
   return !((bz && !az) || (bx && !ax) || (by && !ay));
@@ -351,13 +378,11 @@ __global__ void __launch_bounds__(kRevWarps * 32)
     const long long di = (long long)sz * NXY, dj = (long long)sx * A.NY, dk = sy;
     const long long jk = (long long)j * A.NY + k;
     const long long sbase = (long long)src * A.nodes;
-    const long long tbase = ((long long)e * A.nsrc + src) * A.nodes;
     double* lam_s = A.lam + sbase;
     double* tt_s = A.tt + sbase;
     double* con_s = A.contrib + sbase * kSlots;
     double* g8_s = A.g8 + sbase * 8;
-    const uint8_t* code_s = A.tcode + tbase;
-    const double* old_s = A.told + tbase;
+    const int zsi = A.params[src].zsi, xsi = A.params[src].xsi, ysi = A.params[src].ysi;
     const bool face_j = lj == PJW - 1, face_k = lk == PKW - 1;
     // the cells around this column (rows along i are set per node)
     const long long nxy_c = (long long)A.nx * A.ny;
@@ -407,7 +432,8 @@ __global__ void __launch_bounds__(kRevWarps * 32)
       if (act) {
         const int i = rz > 0 ? r : A.NZ - 1 - r;
         const long long n = (long long)i * NXY + jk;
-        const int code = __ldg(code_s + n);
+        const uint8_t* rec = A.tape.code + (sbase + n) * A.tape.E;
+        const int code = __ldg(rec + e);
         const double lam0 = __ldcg(lam_s + n);
         const bool iin = r > 0;
         if (lj == 0) {
@@ -450,7 +476,8 @@ __global__ void __launch_bounds__(kRevWarps * 32)
             *g = __ldcg(g) + lam * ps;
           }
           lam_s[n] = 0.0;
-          tt_s[n] = __ldg(old_s + n);
+          tt_s[n] = tape_replaced(A.tape, src, sbase + n, rec, e, i, j, k, zsi, xsi, ysi,
+                                  S.status);
         }
         // Slots read by the readers' pencils across the far faces.
         double* co = con_s + n * kSlots;
@@ -573,15 +600,18 @@ __global__ void adj_seed_kernel(const RevArgs A, const double* ax0, const double
 }
 
 // dL/ds per cell: the terms its 8 corner nodes booked for it, summed over the
-// sources in order, plus the receivers' source-cell terms.
-__global__ void adj_gather_kernel(const RevArgs A, const double* vzg, double* grad_slow) {
+// sources in order, plus the receivers' source-cell terms; with `accumulate`,
+// the sum continues from the value already in grad_slow, so a problem split
+// into consecutive source chunks sums in exactly the unsplit order.
+__global__ void adj_gather_kernel(const RevArgs A, const double* vzg, int accumulate,
+                                  double* grad_slow) {
   const long long ncell = (long long)A.nz * A.nx * A.ny;
   const long long NXY = (long long)A.NX * A.NY;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
        c += (long long)gridDim.x * blockDim.x) {
     const int ci = (int)(c / ((long long)A.nx * A.ny));
     const int cj = (int)((c / A.ny) % A.nx), ck = (int)(c % A.ny);
-    double g = 0.0;
+    double g = accumulate ? grad_slow[c] : 0.0;
     for (int s = 0; s < A.nsrc; ++s) {
       const long long base = (long long)s * A.nodes;
       for (int e = 0; e < 8; ++e) {
@@ -633,28 +663,26 @@ extern "C" size_t fteik3d_adjoint_workspace_bytes(int nz, int nx, int ny, int ns
 }
 
 extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, double dz, double dx,
-                               double dy, int nsrc, int nsweep, const double* tt,
-                               const void* solve_workspace, size_t solve_workspace_bytes,
-                               const void* tape, size_t tape_bytes, const double* ax0,
-                               const double* ax1, const double* ax2, const double* sources,
-                               const double* receivers, int nrec, const double* grad_tt_rec,
-                               double* grad_slow, void* workspace, size_t workspace_bytes,
-                               long long spin_limit, void* stream) {
+                               double dy, int nsrc, int nsweep, const double* tt, int history,
+                               const void* tape, size_t tape_bytes,
+                               const double* ax0, const double* ax1, const double* ax2,
+                               const double* sources, const double* receivers, int nrec,
+                               const double* grad_tt_rec, int accumulate, double* grad_slow,
+                               void* workspace, size_t workspace_bytes, long long spin_limit,
+                               void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || nsweep < 0 || nrec < 0 || !slow || !tt ||
-      !solve_workspace || !tape || !ax0 || !ax1 || !ax2 || !sources ||
+      !tape || !ax0 || !ax1 || !ax2 || !sources ||
       (nrec > 0 && (!receivers || !grad_tt_rec)) || !grad_slow || !workspace)
     return kInvalidArgument;
-  const Layout3 S = layout3(nz, nx, ny, nsrc, 2);
-  if (solve_workspace_bytes < S.total) return kWorkspaceTooSmall;
-  if (tape_bytes < fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep)) return kWorkspaceTooSmall;
+  const size_t tape_need = fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep, history);
+  if (tape_need == 0) return kInvalidArgument;
+  if (tape_bytes < tape_need) return kWorkspaceTooSmall;
   const AdjLayout L = adj_layout(nz, nx, ny, nsrc);
   if (workspace_bytes < L.total) return kWorkspaceTooSmall;
-  const char* sw = (const char*)solve_workspace;
   char* ws = (char*)workspace;
   RevArgs A;
   A.slow = slow;
-  A.params = (const Source3*)(sw + S.params);
   A.tt = (double*)(ws + L.tt);
   A.lam = (double*)(ws + L.lam);
   A.contrib = (double*)(ws + L.contrib);
@@ -669,9 +697,9 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
   A.nsrc = nsrc;
   A.o = make_ops3(dz, dx, dy);
   const long long N = A.nodes * nsrc;
-  const size_t ntape = (size_t)N * 8 * (size_t)nsweep;
-  A.tcode = (const uint8_t*)tape;
-  A.told = (const double*)((const char*)tape + align_up(ntape));
+  A.tape = tape_at(const_cast<void*>(tape), tape_layout(nz, nx, ny, nsrc, nsweep, history),
+                   nsweep, history);
+  A.params = A.tape.params;
   double* vzg = (double*)(ws + L.vzg);
 
   FTEIK_CHECK(cudaMemcpyAsync(A.tt, tt, 8 * (size_t)N, cudaMemcpyDeviceToDevice, st));
@@ -705,7 +733,8 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
   }
   FTEIK_CHECK(cudaGetLastError());
   adj_initial_kernel<<<(nsrc * 8 + 127) / 128, 128, 0, st>>>(A);
-  adj_gather_kernel<<<grid_for((long long)nz * nx * ny, 256), 256, 0, st>>>(A, vzg, grad_slow);
+  adj_gather_kernel<<<grid_for((long long)nz * nx * ny, 256), 256, 0, st>>>(A, vzg, accumulate,
+                                                                           grad_slow);
   FTEIK_CHECK(cudaGetLastError());
   FTEIK_CHECK(cudaStreamSynchronize(st));
   if (nepochs > 0) {

@@ -40,6 +40,7 @@ enum Status : int {
   kInvalidArgument = 5,
   kCudaError = 6,
   kWorkspaceTooSmall = 7,
+  kTapeOverflow = 8,
 };
 
 // ---- integer-pipe comparisons -------------------------------------------------

@@ -230,6 +230,34 @@ __device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, do
   return dle(thr, tev) && dle(thr, ten) && dle(thr, tnv) && dle(thr, tnve);
 }
 
+// Tape entry of a change of node sn (= source * nodes + n) in sweep e: its
+// operator code, and the value t0 it replaced unless this is the node's first
+// change (see Tape3).  A full overflow table flags FTEIK_TAPE_OVERFLOW, which
+// also ends the solve early (its waits give up once the status is set): the
+// caller retries with more history slots.
+__device__ __forceinline__ void tape_record(const Tape3& P, int* status, long long sn, int e,
+                                            uint8_t code, double t0) {
+  uint8_t* rec = P.code + sn * P.E;
+  const int m = tape_changes_before(rec, e) + 1;  // this change's number
+  rec[e] = code;
+  if (m < 2) return;
+  if (m - 2 < P.H) {
+    P.hist[sn * P.H + (m - 2)] = t0;
+    return;
+  }
+  const unsigned long long key = tape_key(sn, m);
+  unsigned long long h = tape_slot(key, P.mask);
+  for (int q = 0; q < kTapeProbes; ++q) {
+    const unsigned long long prev = atomicCAS(P.key + h, 0ull, key);
+    if (prev == 0ull || prev == key) {
+      P.val[h] = t0;
+      return;
+    }
+    h = (h + 1) & P.mask;
+  }
+  atomicCAS(status, 0, (int)kTapeOverflow);
+}
+
 // One model of a multi-model launch (device table built by the host).
 struct Model3 {
   Ops3 o;
@@ -258,8 +286,7 @@ struct Sweep3Args {
   Coef3 C;              // precomputed coefficients (COEF variant)
   const double* slow;   // slowness cells (cell variant)
   const int* no_skip;   // set by coef3d_kernel when the all-Big skip is not exact
-  uint8_t* tape_code;   // optional: per sweep, the operator code of every change
-  double* tape_old;     // optional: per sweep, the value each change replaced
+  Tape3 tape;           // optional (tape.code null: none): the adjoint's record of every change
   unsigned* progress;
   const int* order;
   int nz, nx, ny;  // cells
@@ -504,11 +531,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
           if (!deq(res, t0)) {
             tts[n] = res;
             if (GRAD) recs[n] = code;
-            if (!MULTI && A.tape_code) {
-              const long long tq = ((long long)e * A.nsrc + src) * nodes + n;
-              A.tape_code[tq] = code;
-              A.tape_old[tq] = t0;
-            }
+            if (!MULTI && A.tape.code)
+              tape_record(A.tape, A.status, (long long)src * nodes + n, e, code, t0);
           }
         }
       }
@@ -823,11 +847,8 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
         if (!deq(res, t0)) {
           tts[n] = res;
           if (GRAD) recs[n] = code;
-          if (A.tape_code) {
-            const long long tq = ((long long)e * A.nsrc + src) * A.nodes + n;
-            A.tape_code[tq] = code;
-            A.tape_old[tq] = t0;
-          }
+          if (A.tape.code)
+            tape_record(A.tape, A.status, (long long)src * A.nodes + n, e, code, t0);
         }
       }
       r3v = r2v;
@@ -983,6 +1004,20 @@ __global__ void init3d_batch_kernel(const Model3* models, const Job3* jobs, int 
   const Source3 p = init3d_source(M.slow, src + 3 * q, M.nz, M.nx, M.ny, M.o, jb.tt);
   params[q] = p;
   vzero_out[q] = p.vzero;
+}
+
+// The adjoint's tape keeps each source's set-up and the initial values of
+// the 8 nodes around it (the values their first change replaces): one thread
+// per node.
+__global__ void tape_init_kernel(const double* tt, const Source3* params, int nsrc,
+                                 long long nodes, int NX, int NY, Tape3 tape) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsrc * 8) return;
+  const int s = q >> 3, c = q & 7;
+  const Source3 p = params[s];
+  if (c == 0) tape.params[s] = p;
+  const int i = p.zsi + (c & 1), j = p.xsi + ((c >> 1) & 1), k = p.ysi + ((c >> 2) & 1);
+  tape.init8[q] = tt[(long long)s * nodes + ((long long)i * NX + j) * NY + k];
 }
 
 // Fill every node of every job with Big (and its record with "no sign"):
@@ -1235,8 +1270,8 @@ extern "C" size_t fteik3d_workspace_bytes(int nz, int nx, int ny, int nsrc, int 
 static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, double dx,
                         double dy, const double* sources, int nsrc, int nsweep, int grad,
                         double* tt, double* ttgrad, double* vzero, void* workspace,
-                        size_t workspace_bytes, uint8_t* tape_code, double* tape_old,
-                        long long spin_limit, void* stream, const Tune3* force = nullptr) {
+                        size_t workspace_bytes, const Tape3* tape, long long spin_limit,
+                        void* stream, const Tune3* force = nullptr) {
   cudaStream_t st = (cudaStream_t)stream;
   if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || nsweep < 0 || !slow || !sources || !tt ||
       !vzero || !workspace || grad < 0 || grad > 2 || (grad == 1 && !ttgrad))
@@ -1299,6 +1334,9 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
   fill3d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
   init3d_kernel<<<(nsrc + 63) / 64, 64, 0, st>>>(slow, src_dev, nsrc, nz, nx, ny, o, tt, nodes,
                                                  params, vzero);
+  if (tape)
+    tape_init_kernel<<<(nsrc * 8 + 127) / 128, 128, 0, st>>>(tt, params, nsrc, nodes, NX, NY,
+                                                             *tape);
   FTEIK_CHECK(cudaGetLastError());
   if (nsweep > 0) {
     Sweep3Args A;
@@ -1308,8 +1346,7 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
     A.C = C;
     A.slow = slow;
     A.no_skip = no_skip;
-    A.tape_code = tape_code;
-    A.tape_old = tape_old;
+    if (tape) A.tape = *tape;
     A.progress = progress;
     A.ticket = ticket;
     A.status = status;
@@ -1359,30 +1396,33 @@ extern "C" int fteik3d_solve_async(const double* slow, int nz, int nx, int ny, d
                                    double* vzero, void* workspace, size_t workspace_bytes,
                                    long long spin_limit, void* stream) {
   return solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, nsweep, grad, tt, ttgrad,
-                      vzero, workspace, workspace_bytes, nullptr, nullptr, spin_limit, stream);
+                      vzero, workspace, workspace_bytes, nullptr, spin_limit, stream);
 }
 
-extern "C" size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep) {
-  if (nz < 1 || nx < 1 || ny < 1 || nsrc < 1 || nsweep < 0) return 0;
-  const size_t n = (size_t)(nz + 1) * (nx + 1) * (ny + 1) * nsrc * 8 * (size_t)nsweep;
-  return n == 0 ? 256 : align_up(n) + align_up(8 * n);  // nsweep 0: a token buffer
+extern "C" size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep,
+                                     int history) {
+  if (nz < 1 || nx < 1 || ny < 1 || nsrc < 1 || nsweep < 0 || 8 * nsweep > kTapeMaxEpochs ||
+      history < 0 || (nsweep > 0 && history > 8 * nsweep - 1) || (nsweep == 0 && history != 0))
+    return 0;
+  return tape_layout(nz, nx, ny, nsrc, nsweep, history).total;
 }
 
 extern "C" int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, double dz,
                                   double dx, double dy, const double* sources, int nsrc,
                                   int nsweep, double* tt, double* vzero, void* workspace,
-                                  size_t workspace_bytes, void* tape, size_t tape_bytes,
-                                  long long spin_limit, void* stream) {
-  const size_t need = fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep);
+                                  size_t workspace_bytes, int history, void* tape,
+                                  size_t tape_bytes, long long spin_limit, void* stream) {
+  const size_t need = fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep, history);
   if (!tape || need == 0) return kInvalidArgument;
   if (tape_bytes < need) return kWorkspaceTooSmall;
-  const size_t n = (size_t)(nz + 1) * (nx + 1) * (ny + 1) * nsrc * 8 * (size_t)nsweep;
-  uint8_t* code = (uint8_t*)tape;
-  double* old = (double*)((char*)tape + align_up(n));
-  // 255 marks "unchanged in this sweep"
-  if (n) FTEIK_CHECK(cudaMemsetAsync(code, 0xff, n, (cudaStream_t)stream));
+  const TapeLayout L = tape_layout(nz, nx, ny, nsrc, nsweep, history);
+  const Tape3 T = tape_at(tape, L, nsweep, history);
+  cudaStream_t st = (cudaStream_t)stream;
+  // code 255 marks "unchanged in this sweep"; key 0 marks an empty table slot
+  if (L.hist > L.code) FTEIK_CHECK(cudaMemsetAsync(T.code, 0xff, L.hist - L.code, st));
+  FTEIK_CHECK(cudaMemsetAsync(T.key, 0, L.val - L.key, st));
   int rc = solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, nsweep, 2, tt, nullptr,
-                        vzero, workspace, workspace_bytes, code, old, spin_limit, stream);
+                        vzero, workspace, workspace_bytes, &T, spin_limit, stream);
   if (rc != kOk) return rc;
   return fteik_workspace_status(workspace, stream);
 }
@@ -1714,8 +1754,8 @@ extern "C" int fteik3d_autotune(const double* slow, int nz, int nx, int ny, doub
     return timed(
         [&]() {
           int rc = solve3d_impl(slow, nz, nx, ny, dz, dx, dy, sources, nsrc, 1, grad, tt, ttgrad,
-                                vzero, workspace, workspace_bytes, nullptr, nullptr, spin_limit,
-                                stream, &t);
+                                vzero, workspace, workspace_bytes, nullptr, spin_limit, stream,
+                                &t);
           if (rc != kOk) return rc;
           return fteik_workspace_status(workspace, stream);
         },

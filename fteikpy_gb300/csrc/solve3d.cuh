@@ -104,6 +104,117 @@ struct Layout3 {
 
 inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// ---- the adjoint's tape ------------------------------------------------------
+//
+// What the reverse pass needs from the forward sweeps, per source and node:
+// in which sweeps the node changed, with the code of the operator that
+// changed it (the reference's ttsgn triple, _fteik3d.py:166-200), and the
+// value each change replaced.  Most nodes change two or three times in all
+// (about 95% on layered and gradient models at nsweep 2), so the replaced
+// values are kept compactly:
+//   code [nsrc][nodes][E]  E = 8 * nsweep bytes per node, 255 = unchanged in
+//                          that sweep; the count of changes before sweep e is
+//                          the count of codes != 255 at sweeps < e
+//   hist [nsrc][nodes][H]  the value replaced by the node's 2nd .. (H+1)-th
+//                          change (its first change replaces the initial
+//                          value: Big, or the analytic value of the 8 nodes
+//                          around the source, kept in init8)
+//   table                  later changes (rare): an open-addressing table of
+//                          (source node, change number) -> replaced value,
+//                          capacity a power of 2 >= nodes * nsrc / 4; when a
+//                          probe sequence runs past kTapeProbes the solve
+//                          reports FTEIK_TAPE_OVERFLOW (the caller retries
+//                          with a larger H; H = E - 1 never needs the table)
+//   init8 [nsrc][8]        the initial values of the nodes around the source
+//   params [nsrc]          each source's set-up (Source3), for the adjoint
+constexpr int kTapeProbes = 64;
+constexpr int kTapeMaxEpochs = 4095;  // change numbers fit in the key's 12 bits
+
+struct Tape3 {
+  uint8_t* code;
+  double* hist;
+  unsigned long long* key;  // 0: empty slot, else ((source node) << 12 | change) + 1
+  double* val;
+  double* init8;
+  Source3* params;
+  unsigned long long mask;  // table capacity - 1
+  int E, H;
+};
+
+struct TapeLayout {
+  size_t code, hist, key, val, init8, params, total;
+  unsigned long long cap;
+};
+
+inline TapeLayout tape_layout(int nz, int nx, int ny, int nsrc, int nsweep, int history) {
+  const size_t N = (size_t)(nz + 1) * (nx + 1) * (ny + 1) * (size_t)nsrc;
+  const size_t E = 8 * (size_t)nsweep;
+  TapeLayout L;
+  unsigned long long cap = 4096;
+  while (cap < N / 4) cap <<= 1;
+  L.cap = cap;
+  size_t off = 0;
+  L.code = off;
+  off = align_up(off + N * E);
+  L.hist = off;
+  off = align_up(off + N * (size_t)history * 8);
+  L.key = off;
+  off = align_up(off + cap * 8);
+  L.val = off;
+  off = align_up(off + cap * 8);
+  L.init8 = off;
+  off = align_up(off + (size_t)nsrc * 64);
+  L.params = off;
+  off = align_up(off + (size_t)nsrc * sizeof(Source3));
+  L.total = off;
+  return L;
+}
+
+inline Tape3 tape_at(void* base, const TapeLayout& L, int nsweep, int history) {
+  char* b = (char*)base;
+  Tape3 t;
+  t.code = (uint8_t*)(b + L.code);
+  t.hist = (double*)(b + L.hist);
+  t.key = (unsigned long long*)(b + L.key);
+  t.val = (double*)(b + L.val);
+  t.init8 = (double*)(b + L.init8);
+  t.params = (Source3*)(b + L.params);
+  t.mask = L.cap - 1;
+  t.E = 8 * nsweep;
+  t.H = history;
+  return t;
+}
+
+__device__ __forceinline__ unsigned long long tape_key(long long sn, int m) {
+  return (((unsigned long long)sn << 12) | (unsigned)m) + 1ull;
+}
+// First probe slot of a key: MurmurHash3's 64-bit finaliser (fmix64, public
+// domain), so neighbouring nodes spread over the whole table.
+__device__ __forceinline__ unsigned long long tape_slot(unsigned long long key,
+                                                        unsigned long long mask) {
+  unsigned long long h = key;
+  h ^= h >> 33;
+  h *= 0xff51afd7ed558ccdull;
+  h ^= h >> 33;
+  h *= 0xc4ceb9fe1a85ec53ull;
+  h ^= h >> 33;
+  return h & mask;
+}
+
+// Number of sweeps before sweep e (e < E) in which the node with this code
+// record changed.  E is a multiple of 8 and rec is 8-byte aligned.
+__device__ __forceinline__ int tape_changes_before(const uint8_t* rec, int e) {
+  int m = 0;
+  for (int w = 0; w * 8 < e; ++w) {
+    const unsigned long long x = __ldcg((const unsigned long long*)rec + w);
+    const int nb = e - w * 8 < 8 ? e - w * 8 : 8;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+      if (b < nb) m += ((x >> (8 * b)) & 0xffull) != 0xffull;
+  }
+  return m;
+}
+
 inline Layout3 layout3(int nz, int nx, int ny, int nsrc, int grad) {
   const size_t npen = (size_t)max_pencils(nx + 1, ny + 1);
   const size_t nodes = (size_t)(nz + 1) * (nx + 1) * (ny + 1);

@@ -30,6 +30,7 @@ extern "C" {
 #define FTEIK_INVALID_ARGUMENT 5
 #define FTEIK_CUDA_ERROR 6
 #define FTEIK_WORKSPACE_TOO_SMALL 7
+#define FTEIK_TAPE_OVERFLOW 8         /* the adjoint's tape needs more history slots */
 
 /* Library version and a short description of the last CUDA error, if any. */
 const char* fteik_version(void);
@@ -193,40 +194,55 @@ int fteik3d_solve_noalloc(const double* slow, int nz, int nx, int ny, double dz,
  * of a loss on receiver traveltimes with respect to slowness, for tomography.
  *
  * fteik3d_solve_tape runs the same solve as fteik3d_solve (grad = 2: no
- * gradients, branch record kept) and also writes a tape of every sweep: per
- * node, the code of the operator that changed it (the reference's ttsgn
- * encoding, _fteik3d.py:166-200; 255 = unchanged) and the value it replaced.
- * `tape` is a device buffer of fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep)
- * bytes (9 bytes per node, source and directional sweep).
+ * gradients, branch record kept) and also writes a tape of every change the
+ * sweeps make: per node and directional sweep, the code of the operator that
+ * changed it (the reference's ttsgn encoding, _fteik3d.py:166-200; 255 =
+ * unchanged), and the value each change replaced. A node's first change
+ * replaces its initial value (kept for the 8 nodes around the source, Big
+ * elsewhere); the values replaced by its next `history` changes go to per-node
+ * slots, later ones to an overflow table sized for a quarter of the nodes.
+ * `tape` is a device buffer of fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep,
+ * history) bytes: (8 * nsweep + 8 * history + about 4) bytes per node and
+ * source, plus each source's set-up. 0 <= history <= 8 * nsweep - 1 (0 when nsweep = 0); with 2 (about
+ * 95% of the nodes of layered or gradient models change at most 3 times at
+ * nsweep 2) the tape takes 36 bytes per node at nsweep 2, against 144 for a
+ * dense record of every sweep. A problem whose changes overflow the table
+ * returns FTEIK_TAPE_OVERFLOW (its results are then invalid): retry with a
+ * larger history; history = 8 * nsweep - 1 never overflows.
  *
  * fteik3d_adjoint then differentiates exactly the computation that solve ran,
  * sweep by sweep in reverse, so the gradient matches finite differences of
  * the solver for any nsweep, converged or not.
- *  slow, tt, solve_workspace, tape   the inputs and results of that solve
+ *  slow, tt, history, tape   the inputs and results of that solve (the tape
+ *              also keeps each source's set-up, so the solve's workspace may
+ *              be reused once fteik3d_solve_tape returns)
  *  ax0..ax2    device node axes (lengths nz+1, nx+1, ny+1) used for the
  *              receivers' traveltimes (apparent-velocity interpolation)
  *  sources     device [nsrc][3] source coordinates on those axes
  *  receivers   device [nrec][3], the same receivers for every source
  *  grad_tt_rec device [nsrc][nrec] d(loss)/d(traveltime at receiver)
+ *  accumulate  0: grad_slow = the sum over these sources; 1: the sum continues
+ *              from the values in grad_slow, in the same order, so sources
+ *              split into consecutive chunks (each with its own solve and
+ *              tape) give the unsplit result bit for bit
  *  grad_slow   device [nz][nx][ny] d(loss)/d(slowness), summed over sources
  *  spin_limit  polls of one progress wait before the reverse pass gives up
  *              with FTEIK_DEVICE_WAIT_TIMEOUT (<= 0: default)
  * The reverse pass undoes every sweep of every source in one persistent
  * launch, as sweeps against the forward direction in the solve's pencil
  * schedule. Deterministic (no floating-point atomics). Both calls block. */
-size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep);
+size_t fteik3d_tape_bytes(int nz, int nx, int ny, int nsrc, int nsweep, int history);
 int fteik3d_solve_tape(const double* slow, int nz, int nx, int ny, double dz, double dx,
                        double dy, const double* sources, int nsrc, int nsweep, double* tt,
-                       double* vzero, void* workspace, size_t workspace_bytes, void* tape,
-                       size_t tape_bytes, long long spin_limit, void* stream);
+                       double* vzero, void* workspace, size_t workspace_bytes, int history,
+                       void* tape, size_t tape_bytes, long long spin_limit, void* stream);
 size_t fteik3d_adjoint_workspace_bytes(int nz, int nx, int ny, int nsrc);
 int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, double dz, double dx, double dy,
-                    int nsrc, int nsweep, const double* tt, const void* solve_workspace,
-                    size_t solve_workspace_bytes, const void* tape, size_t tape_bytes,
-                    const double* ax0, const double* ax1, const double* ax2,
+                    int nsrc, int nsweep, const double* tt, int history, const void* tape,
+                    size_t tape_bytes, const double* ax0, const double* ax1, const double* ax2,
                     const double* sources, const double* receivers, int nrec,
-                    const double* grad_tt_rec, double* grad_slow, void* workspace,
-                    size_t workspace_bytes, long long spin_limit, void* stream);
+                    const double* grad_tt_rec, int accumulate, double* grad_slow,
+                    void* workspace, size_t workspace_bytes, long long spin_limit, void* stream);
 
 /* ------------------------------------------------------ model preparation --
  * Replace the SciPy calls of Grid*.resample / Grid*.smooth

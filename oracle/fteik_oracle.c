@@ -102,6 +102,62 @@ typedef struct {
   double dz, dx, dy, dz2i, dx2i, dy2i, dz2dx2, dz2dy2, dx2dy2, dsum;
 } dargs3_t;
 
+/* Optional instrumentation of the 3D node updates, for choosing the cells of
+ * the adjoint's finite-difference check (not part of the reference): per
+ * solve, a digest of every discrete decision (which candidate each update
+ * keeps, and which slowness cells attain the minimum its operator takes), and
+ * a flag on every cell that a kept operator's minimum takes within a relative
+ * `margin` of another cell (a tie: there the solve has only one-sided
+ * derivatives in that cell).  Set per thread while a solve runs. */
+typedef struct {
+  unsigned long long digest;
+  uint8_t* tied; /* [cells], or NULL */
+  double margin;
+} probe3_t;
+static _Thread_local probe3_t* g_probe3 = NULL;
+
+static void probe3_update(probe3_t* p, const double* slow, int winner, int i1, int j1, int k1,
+                          int im, int ip, int jm, int jp, int km, int kp, int nx, int ny) {
+  /* the cells of the winner's slowness minimum (_fteik3d.py:78-101,108,121,134,148) */
+  int c[4][3], nc = 0;
+#define PUT(a, b, d) (c[nc][0] = (a), c[nc][1] = (b), c[nc][2] = (d), ++nc)
+  switch (winner) {
+    case 1: PUT(i1, jm, km); PUT(i1, jm, kp); PUT(i1, jp, km); PUT(i1, jp, kp); break;
+    case 2: PUT(im, j1, km); PUT(ip, j1, km); PUT(im, j1, kp); PUT(ip, j1, kp); break;
+    case 3: PUT(im, jm, k1); PUT(im, jp, k1); PUT(ip, jm, k1); PUT(ip, jp, k1); break;
+    case 4: PUT(i1, j1, km); PUT(i1, j1, kp); break;
+    case 5: PUT(i1, jm, k1); PUT(i1, jp, k1); break;
+    case 6: PUT(im, j1, k1); PUT(ip, j1, k1); break;
+    case 7: PUT(i1, j1, k1); break;
+    default: break;
+  }
+#undef PUT
+  const long SXY = (long)(nx - 1) * (ny - 1);
+  const int SY = ny - 1;
+  long idx[4];
+  double v[4], vmin = 0.0;
+  for (int q = 0; q < nc; ++q) {
+    idx[q] = (long)c[q][0] * SXY + (long)c[q][1] * SY + c[q][2];
+    v[q] = slow[idx[q]];
+    vmin = (q == 0 || v[q] < vmin) ? v[q] : vmin;
+  }
+  unsigned mask = 0;
+  int near = 0;
+  for (int q = 0; q < nc; ++q) {
+    if (v[q] == vmin) mask |= 1u << q;
+    int dup = 0;
+    for (int r = 0; r < q; ++r) dup |= idx[r] == idx[q];
+    if (!dup && v[q] <= vmin * (1.0 + p->margin)) ++near;
+  }
+  p->digest = (p->digest ^ (unsigned long long)(winner | (mask << 4))) * 0x100000001b3ull;
+  if (near > 1 && p->tied)
+    for (int q = 0; q < nc; ++q)
+      if (v[q] <= vmin * (1.0 + p->margin)) {
+#pragma omp atomic write
+        p->tied[idx[q]] = 1;
+      }
+}
+
 /* sweep (one node update), _fteik3d.py:38-200.  nz, nx, ny are NODE counts. */
 static void sweep3_node(double* tt, int8_t* sgn, const double* slow, const dargs3_t* d, int i,
                         int j, int k, int sgnvz, int sgnvx, int sgnvy, int sgntz, int sgntx,
@@ -187,6 +243,11 @@ static void sweep3_node(double* tt, int8_t* sgn, const double* slow, const dargs
   double t0 = TT(i, j, k);
   double tnew = pmin4(t0, t1d, t2d, t3d);
   TT(i, j, k) = tnew;
+  if (g_probe3) {
+    int w = tnew == t0 ? 0 : tnew == t1d1 ? 1 : tnew == t1d2 ? 2 : tnew == t1d3 ? 3
+            : tnew == t2d1 ? 4 : tnew == t2d2 ? 5 : tnew == t2d3 ? 6 : 7;
+    probe3_update(g_probe3, slow, w, i1, j1, k1, im, ip, jm, jp, km, kp, nx, ny);
+  }
   if (grad && tnew != t0) {
     long n = ((long)i * NXY + (long)j * ny + k) * 3;
     int a, b, c;
@@ -333,6 +394,32 @@ int oracle_fteik3d_many(const double* slow, int nz, int nx, int ny, double dz, d
     int st = oracle_fteik3d(slow, nz, nx, ny, dz, dx, dy, src[3 * s], src[3 * s + 1],
                             src[3 * s + 2], nsweep, grad, tt + s * nn,
                             grad ? ttgrad + s * nn * 3 : NULL, vzero + s);
+    if (st != ST_OK) {
+#pragma omp critical
+      status = st;
+    }
+  }
+  return status;
+}
+
+/* oracle_fteik3d_many with the instrumentation above: digests[nsrc] of each
+ * solve's decisions, and tied[cells] set on every cell that some source's
+ * kept operator takes within `margin` of a tie (NULL: not wanted). */
+int oracle_fteik3d_probe(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                         double dy, const double* src, int nsrc, int nsweep, double margin,
+                         double* tt, double* vzero, unsigned long long* digests, uint8_t* tied,
+                         int nthreads) {
+  long nn = (long)(nz + 1) * (nx + 1) * (ny + 1);
+  int status = ST_OK;
+  if (tied) memset(tied, 0, (size_t)nz * nx * ny);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) if (nthreads > 1)
+  for (int s = 0; s < nsrc; ++s) {
+    probe3_t p = {0xcbf29ce484222325ull, tied, margin};
+    g_probe3 = &p;
+    int st = oracle_fteik3d(slow, nz, nx, ny, dz, dx, dy, src[3 * s], src[3 * s + 1],
+                            src[3 * s + 2], nsweep, 0, tt + s * nn, NULL, vzero + s);
+    g_probe3 = NULL;
+    digests[s] = p.digest;
     if (st != ST_OK) {
 #pragma omp critical
       status = st;

@@ -50,6 +50,9 @@ def lib(fast=False):
         L.oracle_fteik3d_many.restype = _I
         L.oracle_fteik3d_record.argtypes = [_P, _I, _I, _I, _D, _D, _D, _D, _D, _D, _I, _P, _P, _P, _P]
         L.oracle_fteik3d_record.restype = _I
+        L.oracle_fteik3d_probe.argtypes = [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _D, _P, _P,
+                                           _P, _P, _I]
+        L.oracle_fteik3d_probe.restype = _I
         L.oracle_adjoint3d.argtypes = [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _P, _I, _P, _P, _I]
         L.oracle_adjoint3d.restype = _I
         L.oracle_fteik2d_many.argtypes = [_P, _I, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _I]
@@ -111,6 +114,33 @@ def solve3d_record(slow, gridsize, source, nsweep=2):
     if st == 1:
         raise ValueError("source out of bound")
     return tt, tg, float(vz[0]), sgn
+
+
+def solve3d_probe(slow, gridsize, sources, nsweep=2, margin=0.0, tied=True, nthreads=None):
+    """``solve3d`` (no gradients) that also returns, per source, a digest of
+    every discrete decision of the sweeps (the candidate each node update
+    keeps and the slowness cells attaining its operator's minimum), and the
+    cells that a kept operator's minimum takes within a relative ``margin``
+    of another cell (ties: one-sided derivatives there).
+
+    Returns (tt, vzero, digests[nsrc] uint64, tied[nz, nx, ny] bool or None).
+    Test infrastructure for choosing finite-difference cells of the adjoint
+    check; it is not a restatement of a reference function."""
+    slow = _c(slow)
+    src = _c(np.atleast_2d(sources))
+    nz, nx, ny = slow.shape
+    nsrc = len(src)
+    tt = np.empty((nsrc, nz + 1, nx + 1, ny + 1))
+    vz = np.empty(nsrc)
+    dig = np.zeros(nsrc, dtype=np.uint64)
+    t = np.zeros(slow.shape, dtype=np.uint8) if tied else None
+    st = lib().oracle_fteik3d_probe(
+        _p(slow), nz, nx, ny, *map(float, gridsize), _p(src), nsrc, int(nsweep), float(margin),
+        _p(tt), _p(vz), _p(dig), _p(t) if tied else None, int(nthreads or os.cpu_count()),
+    )
+    if st == 1:
+        raise ValueError("source out of bound")
+    return tt, vz, dig, (t.astype(bool) if tied else None)
 
 
 def adjoint3d(slow, gridsize, sources, nsweep, receivers, grad_tt_rec, nthreads=None):

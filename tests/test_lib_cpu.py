@@ -57,6 +57,47 @@ def test_workspace_sizes(lib):
         assert b % 256 == 0
 
 
+def test_tape_sizes_and_history_limits(lib):
+    """The adjoint's tape: 8 * nsweep code bytes and 8 * history value bytes
+    per node and source, plus the overflow table (a power of 2 of at least a
+    quarter of the nodes, 16 bytes a slot) and per-source set-up; history is
+    at most 8 * nsweep - 1 (0 without sweeps)."""
+    nodes = 5 * 6 * 7
+    n = nodes * 3
+    cap = 4096
+    while cap < n // 4:
+        cap *= 2
+    for nsweep, history in ((2, 2), (1, 7), (3, 0)):
+        b = lib.fteik3d_tape_bytes(4, 5, 6, 3, nsweep, history)
+        assert b % 256 == 0
+        assert b >= n * (8 * nsweep + 8 * history) + 16 * cap + 3 * (64 + 48)
+    big = 64 * 129 * 129 * 97
+    assert lib.fteik3d_tape_bytes(96, 128, 128, 64, 2, 2) < 40 * big  # dense: 144 per node
+    assert lib.fteik3d_tape_bytes(4, 5, 6, 3, 2, 16) == 0
+    assert lib.fteik3d_tape_bytes(4, 5, 6, 3, 2, -1) == 0
+    assert lib.fteik3d_tape_bytes(4, 5, 6, 3, 0, 0) > 0
+    assert lib.fteik3d_tape_bytes(4, 5, 6, 3, 0, 1) == 0
+    assert lib.fteik3d_tape_bytes(4, 5, 6, 3, 512, 2) == 0  # change numbers beyond 12 bits
+    with pytest.raises(RuntimeError, match="tape overflowed"):
+        _lib.check(_lib.TAPE_OVERFLOW)
+
+
+def test_adjoint_chunk_plan():
+    """Sources per chunk halve until one chunk's traveltimes, tape and
+    workspaces fit the budget (never below one source)."""
+    from fteikpy_gb300 import _adjoint
+
+    lib = _lib.load()
+    k, need = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, 1 << 50)
+    assert k == 64
+    k2, need2 = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, need // 3)
+    assert k2 == 16 and need2 <= need // 3
+    assert _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, 1)[0] == 1
+    assert _adjoint._history_steps(2) == [2, 6, 15]
+    assert _adjoint._history_steps(1) == [2, 6, 7]
+    assert _adjoint._history_steps(0) == [0]
+
+
 FAKE = ctypes.c_void_p(0x1000)  # never dereferenced: the calls fail host-side first
 
 

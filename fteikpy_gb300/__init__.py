@@ -12,6 +12,7 @@ from ._grid import Grid2D, Grid3D, TraveltimeGrid2D, TraveltimeGrid3D
 from ._helpers import get_num_threads, set_num_threads
 from ._solver import Eikonal2D, Eikonal3D, autotune, solve_batch
 from ._adjoint import converged, traveltimes
+from ._shard import shard_bounds, sharded_traveltimes, solve_sharded
 from ._io import grid_to_meshio, ray_to_meshio
 
 __all__ = [
@@ -30,5 +31,8 @@ __all__ = [
     "traveltimes",
     "get_num_threads",
     "set_num_threads",
+    "shard_bounds",
+    "sharded_traveltimes",
+    "solve_sharded",
     "__version__",
 ]

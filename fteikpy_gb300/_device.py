@@ -58,7 +58,9 @@ _workspaces = {}
 
 
 def workspace(key, nbytes):
-    ws = _workspaces.setdefault(key, Workspace())
+    """The growable scratch buffer ``key`` of the current device (one per
+    device, so that solves on several devices at once keep their own)."""
+    ws = _workspaces.setdefault((key, device().index), Workspace())
     return ws.get(nbytes)
 
 

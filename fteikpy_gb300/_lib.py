@@ -60,6 +60,8 @@ SIGNATURES = {
     "fteik_correlate1d": (_I, [_I, _P, _P, _I, _P, _I, _P, _P]),
     "fteik2d_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
     "fteik2d_solve": (_I, [_P, _I, _I, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _P]),
+    "fteik2d_chain_stats": (_I, [_P, ctypes.POINTER(ctypes.c_ulonglong),
+                                 ctypes.POINTER(ctypes.c_ulonglong), _P]),
     "fteik_interp3d": (_I, [_P, _I, _P, _I, _P, _I, _P, _LL, _P, _I, _D, _P, _P]),
     "fteik_interp2d": (_I, [_P, _I, _P, _I, _P, _LL, _P, _I, _D, _P, _P]),
     "fteik_vinterp3d": (_I, [_P, _I, _P, _I, _P, _I, _P, _LL, _P, _P, _I, _P, _P, _D, _P, _P]),

@@ -489,58 +489,34 @@ struct Pre2 {
   double vv[kChunk2];    // vref * vref
   double d3[kChunk2];    // the third operator's guard bound
   double t2[kChunk2];    // the second operator's value, where it applies
+  // Speculation: the whole update of the row evaluated with tv equal to the
+  // previous node's value before this pass (tvs), giving tns and its branch
+  // code cds.  When the previous node keeps its value in the pass (most
+  // nodes of most passes), the chain's actual tv has the same bits as tvs
+  // and lane 0 takes the result instead of evaluating the operators.
+  double tvs[kChunk2], tns[kChunk2];
   unsigned char flags[kChunk2];  // 1: tev <= te; 2: the second operator applies
+  unsigned char cds[kChunk2];
 };
-
-template <bool K>
-__device__ __forceinline__ void precompute_row2d(Pre2& P, int q, const double* tt,
-                                                 const double* slow, const Ops2& o, int i, int j,
-                                                 int sgnvz, int sgnvx, int sgntz, int sgntx,
-                                                 int NZ, int NX) {
-  const In2 in = load_in2(tt, slow, i, j, sgnvz, sgnvx, sgntz, sgntx, NZ, NX);
-  const double te = in.te, tev = in.tev;
-  P.a1[q] = o.dz * pmin(in.sz0, in.sz1);
-  P.t1d2[q] = te + o.dx * pmin(in.sx0, in.sx1);
-  const double vref = in.s2;
-  P.c1[q] = te + o.dx * vref;
-  P.b[q] = o.dz * vref;
-  P.p1[q] = tev + te;
-  P.p2[q] = tev - te;
-  const double vv = vref * vref;
-  P.vv[q] = vv;
-  P.x[q] = times4(vv) * o.s2;
-  P.te[q] = te;
-  P.tev[q] = tev;
-  P.vref[q] = vref;
-  P.d3[q] = div_by(o.dxx * vref, o.rhyp);
-  unsigned f = le2<K>(tev, te) ? 1u : 0u;
-  const double dte = te - tev;
-  if (le2<K>(dte, div_by(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, dte)) {
-    const double r = div_by(dte, o.rdz);
-    P.t2[q] = te + o.dx * sqrt(vv - r * r);
-    f |= 2u;
-  }
-  P.flags[q] = (unsigned char)f;
-}
 
 // The precomputed terms the chain reads on every node, loaded into registers
 // one node ahead (the rarer branches read shared memory directly).
 struct Row2 {
-  double a1, t1d2, c1, b, p1, p2, x, te, tev;
-  unsigned flags;
+  double a1, t1d2, c1, b, p1, p2, x, te, tev, tvs, tns;
+  unsigned flags, cds;
 };
 __device__ __forceinline__ Row2 load_row2(const Pre2& P, int q) {
-  return Row2{P.a1[q], P.t1d2[q], P.c1[q], P.b[q], P.p1[q], P.p2[q],
-              P.x[q],  P.te[q],   P.tev[q], P.flags[q]};
+  return Row2{P.a1[q], P.t1d2[q], P.c1[q], P.b[q],   P.p1[q],    P.p2[q],    P.x[q],
+              P.te[q], P.tev[q],  P.tvs[q], P.tns[q], P.flags[q], P.cds[q]};
 }
 
 // node_update2d on precomputed row q: only the terms that involve tv.
+// Returns the node's value after the update and, when it changes, its branch
+// code (GRAD).
 template <bool GRAD, bool K>
-__device__ __forceinline__ double chain_node2d(double* tt, uint8_t* rec, const Ops2& o,
-                                               const Source2& sp, const Pre2& P, const Row2& R,
-                                               int q, int i, int j, int sgntz, int sgntx, int NX,
-                                               double tv, double t0) {
-  const long long n = (long long)i * NX + j;
+__device__ __forceinline__ double eval_node2d(const Ops2& o, const Source2& sp, const Pre2& P,
+                                              const Row2& R, int q, int i, int j, int sgntz,
+                                              int sgntx, double tv, double t0, unsigned& code) {
   const double t1d1 = tv + R.a1;
   const double t1d2 = R.t1d2;
   const double t1d = lt2<K>(t1d2, t1d1) ? t1d2 : t1d1;
@@ -578,29 +554,70 @@ __device__ __forceinline__ double chain_node2d(double* tt, uint8_t* rec, const O
   double tnew = t0;
   if (lt2<K>(t1d, tnew)) tnew = t1d;
   if (lt2<K>(t2d, tnew)) tnew = t2d;
-  if (!eq2<K>(tnew, t0)) {
-    tt[n] = tnew;
-    if (GRAD) {
-      int a, bb;
-      if (eq2<K>(tnew, t1d1)) {
-        a = sgntz; bb = 0;
-      } else if (eq2<K>(tnew, t1d2)) {
-        a = 0; bb = sgntx;
-      } else {
-        a = sgntz; bb = sgntx;
-      }
-      rec[n] = (uint8_t)((a + 1) * 3 + (bb + 1));
+  if (GRAD && !eq2<K>(tnew, t0)) {
+    int a, bb;
+    if (eq2<K>(tnew, t1d1)) {
+      a = sgntz; bb = 0;
+    } else if (eq2<K>(tnew, t1d2)) {
+      a = 0; bb = sgntx;
+    } else {
+      a = sgntz; bb = sgntx;
     }
+    code = (unsigned)((a + 1) * 3 + (bb + 1));
   }
   return tnew;
 }
 
+template <bool GRAD, bool K, bool SPEC>
+__device__ __forceinline__ void precompute_row2d(Pre2& P, int q, const double* tt,
+                                                 const double* slow, const Ops2& o,
+                                                 const Source2& sp, int i, int j, int sgnvz,
+                                                 int sgnvx, int sgntz, int sgntx, int NZ,
+                                                 int NX) {
+  const In2 in = load_in2(tt, slow, i, j, sgnvz, sgnvx, sgntz, sgntx, NZ, NX);
+  const double te = in.te, tev = in.tev;
+  P.a1[q] = o.dz * pmin(in.sz0, in.sz1);
+  P.t1d2[q] = te + o.dx * pmin(in.sx0, in.sx1);
+  const double vref = in.s2;
+  P.c1[q] = te + o.dx * vref;
+  P.b[q] = o.dz * vref;
+  P.p1[q] = tev + te;
+  P.p2[q] = tev - te;
+  const double vv = vref * vref;
+  P.vv[q] = vv;
+  P.x[q] = times4(vv) * o.s2;
+  P.te[q] = te;
+  P.tev[q] = tev;
+  P.vref[q] = vref;
+  P.d3[q] = div_by(o.dxx * vref, o.rhyp);
+  unsigned f = le2<K>(tev, te) ? 1u : 0u;
+  const double dte = te - tev;
+  if (le2<K>(dte, div_by(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, dte)) {
+    const double r = div_by(dte, o.rdz);
+    P.t2[q] = te + o.dx * sqrt(vv - r * r);
+    f |= 2u;
+  }
+  P.flags[q] = (unsigned char)f;
+  if (SPEC) {
+    // this lane's own writes above are visible to it
+    const double tvs = tt[(long long)(i - sgntz) * NX + j];
+    unsigned code = 0;
+    P.tvs[q] = tvs;
+    P.tns[q] = eval_node2d<GRAD, K>(o, sp, P, load_row2(P, q), q, i, j, sgntz, sgntx, tvs,
+                                    in.t0, code);
+    P.cds[q] = (unsigned char)code;
+  }
+}
+
 // One pass over column j (rows i0, i0 + sgntz, ..., i1) by the whole warp.
-template <bool GRAD, bool K>
+// With SPEC, a row whose speculated tv has the bits of the actual one takes
+// the speculated result (the same operations on the same operands, so the
+// same bits); `hits` counts them.
+template <bool GRAD, bool K, bool SPEC>
 __device__ __forceinline__ void warp_pass2d(Pre2& P, double* tt, uint8_t* rec, const double* slow,
                                             const Ops2& o, const Source2& sp, int j, int i0,
                                             int i1, int sgnvz, int sgnvx, int sgntz, int sgntx,
-                                            int NZ, int NX) {
+                                            int NZ, int NX, unsigned long long& hits) {
   const int lane = threadIdx.x & 31;
   const int step = sgntz;
   const int len = (i1 - i0) * step + 1;
@@ -609,8 +626,8 @@ __device__ __forceinline__ void warp_pass2d(Pre2& P, double* tt, uint8_t* rec, c
   for (int c0 = 0; c0 < len; c0 += kChunk2) {
     const int m = imin(kChunk2, len - c0);
     for (int q = lane; q < m; q += 32)
-      precompute_row2d<K>(P, q, tt, slow, o, i0 + (c0 + q) * step, j, sgnvz, sgnvx, sgntz,
-                          sgntx, NZ, NX);
+      precompute_row2d<GRAD, K, SPEC>(P, q, tt, slow, o, sp, i0 + (c0 + q) * step, j, sgnvz,
+                                      sgnvx, sgntz, sgntx, NZ, NX);
     __syncwarp();
     if (lane == 0) {
       int i = i0 + c0 * step;
@@ -623,37 +640,59 @@ __device__ __forceinline__ void warp_pass2d(Pre2& P, double* tt, uint8_t* rec, c
           t0n = tt[(long long)(i + step) * NX + j];
           rn = load_row2(P, q + 1);
         }
-        tv = chain_node2d<GRAD, K>(tt, rec, o, sp, P, r, q, i, j, sgntz, sgntx, NX, tv, t0);
+        unsigned code;
+        double tnew;
+        if (SPEC && deq(tv, r.tvs)) {
+          tnew = r.tns;
+          code = r.cds;
+          ++hits;
+        } else {
+          tnew = eval_node2d<GRAD, K>(o, sp, P, r, q, i, j, sgntz, sgntx, tv, t0, code);
+        }
+        if (!eq2<K>(tnew, t0)) {
+          const long long n = (long long)i * NX + j;
+          tt[n] = tnew;
+          if (GRAD) rec[n] = (uint8_t)code;
+        }
+        tv = tnew;
       }
     }
     __syncwarp();
   }
 }
 
-template <bool GRAD, bool K>
+template <bool GRAD, bool K, bool SPEC>
 __device__ __noinline__ void warp_sweeps2d(Pre2& P, double* tt, uint8_t* rec, const double* slow,
                                            const Ops2& o, const Source2& sp, int nsweep, int NZ,
-                                           int NX) {
+                                           int NX, unsigned long long* stats) {
+  unsigned long long hits = 0;
   for (int sw = 0; sw < nsweep; ++sw) {
     for (int j = 1; j < NX; ++j) {
-      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX);
-      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX);
+      warp_pass2d<GRAD, K, SPEC>(P, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX, hits);
+      warp_pass2d<GRAD, K, SPEC>(P, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX,
+                                 hits);
     }
     for (int j = NX - 2; j >= 0; --j) {
-      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX);
-      warp_pass2d<GRAD, K>(P, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX);
+      warp_pass2d<GRAD, K, SPEC>(P, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX,
+                                 hits);
+      warp_pass2d<GRAD, K, SPEC>(P, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX,
+                                 hits);
     }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(stats, (unsigned long long)nsweep * 4ull * (unsigned long long)(NZ - 1) * (NX - 1));
+    atomicAdd(stats + 1, hits);
   }
 }
 
 // One warp per source (blockIdx.x): lane 0 runs the first propagation, the
 // warp checks it for non-finite values, then the sweeps run as above.
-template <bool GRAD>
+template <bool GRAD, bool SPEC>
 __global__ void __launch_bounds__(32) solve2d_warp_kernel(const double* slow, const double* src,
                                                           int nz, int nx, int nsweep, Ops2 o,
                                                           double* tt_all, uint8_t* rec_all,
                                                           Source2* params, double* vzero_out,
-                                                          bool keys) {
+                                                          bool keys, unsigned long long* stats) {
   __shared__ Pre2 P;
   __shared__ Source2 sps;
   const int s = blockIdx.x;
@@ -679,9 +718,9 @@ __global__ void __launch_bounds__(32) solve2d_warp_kernel(const double* slow, co
       finite = finite && is_finite(tt[(long long)ii * NX + c]);
   finite = __all_sync(0xffffffffu, finite) && keys;
   if (finite)
-    warp_sweeps2d<GRAD, true>(P, tt, rec, slow, o, sp, nsweep, NZ, NX);
+    warp_sweeps2d<GRAD, true, SPEC>(P, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
   else
-    warp_sweeps2d<GRAD, false>(P, tt, rec, slow, o, sp, nsweep, NZ, NX);
+    warp_sweeps2d<GRAD, false, SPEC>(P, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
 }
 
 __global__ void fill2d_kernel(double* tt, uint8_t* rec, long long n) {
@@ -732,8 +771,8 @@ static Layout2 layout2(int nz, int nx, int nsrc, int grad) {
   const size_t nodes = (size_t)(nz + 1) * (nx + 1);
   Layout2 L;
   size_t off = 0;
-  L.status = off;
-  off = align_up2(off + 16);
+  L.status = off;  // int status; then at byte 8 the chain statistics (u64 nodes, u64 hits)
+  off = align_up2(off + 32);
   L.params = off;
   off = align_up2(off + sizeof(Source2) * (size_t)nsrc);
   L.src = off;
@@ -775,7 +814,7 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
   uint8_t* rec = grad ? (uint8_t*)(ws + L.rec) : nullptr;
   const long long nodes = (long long)(nz + 1) * (nx + 1);
   const long long ntot = nodes * nsrc;
-  FTEIK_CHECK(cudaMemsetAsync(ws + L.status, 0, 16, st));
+  FTEIK_CHECK(cudaMemsetAsync(ws + L.status, 0, 32, st));
   FTEIK_CHECK(cudaMemcpyAsync(src_dev, sources, sizeof(double) * 2 * (size_t)nsrc,
                               cudaMemcpyHostToDevice, st));
   fill2d_kernel<<<grid_for(ntot, 256), 256, 0, st>>>(tt, rec, ntot);
@@ -786,13 +825,18 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
   // thread per source, where each warp instruction serves 32 chains.
   const long long warp_opt = option_value(kOptSweep2dWarp);
   const bool per_warp = warp_opt >= 0 ? warp_opt != 0 : nsrc <= 4 * sm_count();
+  const bool spec = option_value(kOptSweep2dSpec) != 0;
+  unsigned long long* stats = (unsigned long long*)(ws + L.status + 8);
   if (per_warp) {
-    if (grad)
-      solve2d_warp_kernel<true><<<nsrc, 32, 0, st>>>(slow, src_dev, nz, nx, nsweep, o, tt, rec,
-                                                     params, vzero, keys);
-    else
-      solve2d_warp_kernel<false><<<nsrc, 32, 0, st>>>(slow, src_dev, nz, nx, nsweep, o, tt, rec,
-                                                      params, vzero, keys);
+#define FTEIK_W2(G, S)                                                                  \
+  solve2d_warp_kernel<G, S><<<nsrc, 32, 0, st>>>(slow, src_dev, nz, nx, nsweep, o, tt, rec, \
+                                                 params, vzero, keys, stats)
+    if (grad) {
+      if (spec) FTEIK_W2(true, true); else FTEIK_W2(true, false);
+    } else {
+      if (spec) FTEIK_W2(false, true); else FTEIK_W2(false, false);
+    }
+#undef FTEIK_W2
   } else if (grad) {
     solve2d_kernel<true><<<blocks, 32, 0, st>>>(slow, src_dev, nsrc, nz, nx, nsweep, o, tt, rec,
                                                  params, vzero, keys);
@@ -807,4 +851,16 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
     FTEIK_CHECK(cudaGetLastError());
   }
   return fteik_workspace_status(workspace, stream);
+}
+
+extern "C" int fteik2d_chain_stats(const void* workspace, unsigned long long* nodes,
+                                   unsigned long long* hits, void* stream) {
+  if (!workspace || !nodes || !hits) return kInvalidArgument;
+  unsigned long long v[2] = {0, 0};
+  FTEIK_CHECK(cudaMemcpyAsync(v, (const char*)workspace + 8, sizeof(v), cudaMemcpyDeviceToHost,
+                              (cudaStream_t)stream));
+  FTEIK_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+  *nodes = v[0];
+  *hits = v[1];
+  return kOk;
 }

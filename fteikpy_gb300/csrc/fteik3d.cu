@@ -575,11 +575,29 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 // results are known, saves two barriers per step but measured slower.)
 // Operators and their operands are the same as in node_update3d, so results
 // are bit-identical; only which lane evaluates an operator changes.
-constexpr int kTeamWarps = 4;
+#ifndef FTEIK_TEAM_WARPS
+#define FTEIK_TEAM_WARPS 4
+#endif
+constexpr int kTeamWarps = FTEIK_TEAM_WARPS;
 // Resident team blocks per SM the registers are budgeted for.
 #ifndef FTEIK_TEAM_MIN_BLOCKS
 #define FTEIK_TEAM_MIN_BLOCKS 7
 #endif
+
+// Job q of a block's queue, whose warps queued n[0], n[1], ... jobs in
+// turn: the warp w that queued it and its index l in that warp's list.
+__device__ __forceinline__ void team_job(const int (&pre)[kTeamWarps + 1], int q, int& w,
+                                         int& l) {
+  w = 0;
+  int base = 0;
+#pragma unroll
+  for (int x = 1; x < kTeamWarps; ++x)
+    if (q >= pre[x]) {
+      w = x;
+      base = pre[x];
+    }
+  l = q - base;
+}
 
 struct TeamShared {
   // plane jobs, warp w's in [w][0, n2[w]): plane, lane and inputs (u, w, x, q4)
@@ -790,11 +808,15 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
       __syncthreads();
       // ---- stage B: the queued plane operators, 32 jobs per warp instruction ----
       {
-        const int c0 = sh.n2[0], c1 = c0 + sh.n2[1], c2 = c1 + sh.n2[2], c3 = c2 + sh.n2[3];
+        int pre[kTeamWarps + 1];
+        pre[0] = 0;
+#pragma unroll
+        for (int x = 0; x < kTeamWarps; ++x) pre[x + 1] = pre[x] + sh.n2[x];
+        const int c3 = pre[kTeamWarps];
         for (int q = warp * 32 + lane; q - lane < c3; q += kTeamWarps * 32) {
           if (q < c3) {
-            const int w = q < c0 ? 0 : q < c1 ? 1 : q < c2 ? 2 : 3;
-            const int l = q - (w == 0 ? 0 : w == 1 ? c0 : w == 2 ? c1 : c2);
+            int w, l;
+            team_job(pre, q, w, l);
             const int id = sh.jid[w][l];
             sh.r2[w][id >> 5][id & 31] =
                 plane3(id >> 5, sh.ju[w][l], sh.jw[w][l], sh.jx[w][l], sh.jq[w][l], o);
@@ -827,11 +849,15 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
       __syncthreads();
       // ---- stage D: 3D operators ----
       {
-        const int c0 = sh.n3[0], c1 = c0 + sh.n3[1], c2 = c1 + sh.n3[2], c3 = c2 + sh.n3[3];
+        int pre[kTeamWarps + 1];
+        pre[0] = 0;
+#pragma unroll
+        for (int x = 0; x < kTeamWarps; ++x) pre[x + 1] = pre[x] + sh.n3[x];
+        const int c3 = pre[kTeamWarps];
         for (int q = warp * 32 + lane; q - lane < c3; q += kTeamWarps * 32) {
           if (q < c3) {
-            const int w = q < c0 ? 0 : q < c1 ? 1 : q < c2 ? 2 : 3;
-            const int l = q - (w == 0 ? 0 : w == 1 ? c0 : w == 2 ? c1 : c2);
+            int w, l;
+            team_job(pre, q, w, l);
             sh.r3[w][sh.kid[w][l]] =
                 op3d(sh.kin[0][w][l], sh.kin[1][w][l], sh.kin[2][w][l], sh.kin[3][w][l],
                      sh.kin[4][w][l], sh.kin[5][w][l], sh.kin[6][w][l], sh.kin[7][w][l], o);

@@ -41,7 +41,8 @@ enum Option : int {
   kOptAdjointChunk = 5, // adjoint reverse sweeps: steps between progress publications
   kOptSweep2dKeys = 6,  // 2D sweeps: 0 forces IEEE comparisons (else integer keys when exact)
   kOptSweep2dWarp = 7,  // 2D sweeps: 1 one warp per source, 0 one thread per source
-  kOptCount = 8,
+  kOptSweep2dSpec = 8,  // 2D warp sweeps: 0 turns off the speculated updates (same results)
+  kOptCount = 9,
 };
 long long option_value(int opt);
 

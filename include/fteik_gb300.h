@@ -59,6 +59,9 @@ int fteik_kernel_timing(int on);
  * "sweep2d_warp": 1 runs each 2D source on a warp (the warp precomputes the
  * terms of each column that do not depend on the previous node, one lane
  * runs the chain; the default up to 4 sources per SM), 0 on one thread.
+ * "sweep2d_speculate": 0 turns off the warp kernel's speculated updates (each
+ * row also evaluated with the previous node's value from before the pass,
+ * taken when the chain's actual value has the same bits).
  * Results are identical for every setting.
  * fteik_get_option reads a knob back. */
 int fteik_set_option(const char* name, long long value);
@@ -275,6 +278,11 @@ int fteik2d_solve(const double* slow, int nz, int nx, double dz, double dx,
                   const double* sources, int nsrc, int nsweep, int grad, double* tt,
                   double* ttgrad, double* vzero, void* workspace, size_t workspace_bytes,
                   void* stream);
+/* No counterpart in the reference (a measurement hook): after a 2D solve that
+ * ran one warp per source, the node updates of its chains and how many of
+ * them took the speculated result (see "sweep2d_speculate"). Blocking. */
+int fteik2d_chain_stats(const void* workspace, unsigned long long* nodes,
+                        unsigned long long* hits, void* stream);
 
 /* ---------------------------------------------------------- interpolation --
  * interp3d / interp2d (fteikpy/_interp/_interp3d.py:188-195,

@@ -187,3 +187,21 @@ def test_team_kernel_equals_warp_kernel_on_a_layered_model(options, nsrc):
     assert bitwise(out[0][0], out[1][0]) and bitwise(out[0][1], out[1][1])
     tt_o, tg_o, _ = O.solve3d(1.0 / v, d, src, 2, True)
     assert bitwise(out[1][0], tt_o) and bitwise(out[1][1], tg_o)
+
+
+def test_solve_sharded_on_the_visible_devices_equals_one_solve():
+    """The source list split over the visible devices (one here) gives the
+    single solve's results, in source order, bit for bit."""
+    rng = np.random.default_rng(21)
+    shape, d = (14, 18, 22), (10.0, 10.0, 10.0)
+    v = 1500.0 + 40.0 * np.arange(shape[0])[:, None, None] * np.ones(shape)
+    v *= 1.0 + 0.05 * rng.uniform(-1, 1, shape)
+    src = np.column_stack([rng.uniform(0, 140, 5), rng.uniform(0, 180, 5), rng.uniform(0, 220, 5)])
+    eik = fp.Eikonal3D(v, d)
+    one = eik.solve(src, nsweep=2, return_gradient=True)
+    out = fp.solve_sharded(eik, src, nsweep=2, return_gradient=True)
+    assert len(out) == len(one)
+    for a, b in zip(out, one):
+        assert np.array_equal(a.grid, b.grid)
+        assert np.array_equal(a.gradient_tensor.cpu().numpy(), b.gradient_tensor.cpu().numpy())
+        assert np.array_equal(a.source, b.source)

@@ -60,12 +60,18 @@ def test_config1_plain_2d_both_kernels_and_analytic():
     v, v0, src, d = bench.config1_models()
     ref = O.solve2d(1.0 / v, d, [src], 2, False)[0][0]
     try:
-        for warp in (1, 0):  # one warp per source, one thread per source
-            assert lib.fteik_set_option(b"sweep2d_warp", warp) == _lib.OK
-            got = fp.Eikonal2D(v, d).solve(src, nsweep=2).grid
-            assert np.array_equal(got, ref), warp
+        # one warp per source with and without speculated updates, one thread
+        # per source; integer-key and IEEE comparisons
+        for warp, spec in ((1, -1), (1, 0), (0, -1)):
+            for keys in (-1, 0):
+                assert lib.fteik_set_option(b"sweep2d_warp", warp) == _lib.OK
+                assert lib.fteik_set_option(b"sweep2d_speculate", spec) == _lib.OK
+                assert lib.fteik_set_option(b"sweep2d_keys", keys) == _lib.OK
+                got = fp.Eikonal2D(v, d).solve(src, nsweep=2).grid
+                assert np.array_equal(got, ref), (warp, spec, keys)
     finally:
-        lib.fteik_set_option(b"sweep2d_warp", -1)
+        for name in (b"sweep2d_warp", b"sweep2d_speculate", b"sweep2d_keys"):
+            lib.fteik_set_option(name, -1)
     t0 = fp.Eikonal2D(v0, d).solve(src, nsweep=2).grid
     assert np.array_equal(t0, O.solve2d(1.0 / v0, d, [src], 2, False)[0][0])
     ta, far = bench.linear_gradient_times(v0.shape, d, src)

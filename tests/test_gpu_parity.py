@@ -250,24 +250,40 @@ def test_solve3d_batched_equals_single(nsrc):
         ((13, 90), (10.0, 10.0), 3, 1, 3),
     ],
 )
+# 2D kernels: (sweep2d_warp, sweep2d_speculate) -- one warp per source with
+# speculated updates (the default for few sources), the same without them,
+# one thread per source
+KERNELS_2D = {"warp": (1, -1), "warp_nospec": (1, 0), "thread": (0, -1)}
+
+
+def _set_2d(lib, keys, kernel):
+    warp, spec = KERNELS_2D[kernel]
+    assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
+    assert lib.fteik_set_option(b"sweep2d_warp", warp) == 0
+    assert lib.fteik_set_option(b"sweep2d_speculate", spec) == 0
+
+
+def _reset_2d(lib):
+    for name in (b"sweep2d_keys", b"sweep2d_warp", b"sweep2d_speculate"):
+        lib.fteik_set_option(name, -1)
+
+
 @pytest.mark.parametrize("keys", [-1, 0])
-@pytest.mark.parametrize("warp", [1, 0])
-def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys, warp):
+@pytest.mark.parametrize("kernel", list(KERNELS_2D))
+def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys, kernel):
     """Both 2D kernels (one warp per source with the rows' tv-independent terms
-    precomputed by the warp, the default for few sources; one thread per
-    source) and both comparison paths (integer keys, the default for sources
-    whose first propagation is finite; IEEE comparisons) against the oracle,
-    bit for bit."""
+    precomputed by the warp, with and without the speculated updates, the
+    default for few sources; one thread per source) and both comparison paths
+    (integer keys, the default for sources whose first propagation is finite;
+    IEEE comparisons) against the oracle, bit for bit."""
     from fteikpy_gb300 import _lib
 
     lib = _lib.load()
-    assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
-    assert lib.fteik_set_option(b"sweep2d_warp", warp) == 0
+    _set_2d(lib, keys, kernel)
     try:
         _solve2d_bitwise_case(shape, d, nsrc, nsweep, seed)
     finally:
-        lib.fteik_set_option(b"sweep2d_keys", -1)
-        lib.fteik_set_option(b"sweep2d_warp", -1)
+        _reset_2d(lib)
 
 
 def _solve2d_bitwise_case(shape, d, nsrc, nsweep, seed):
@@ -458,8 +474,8 @@ def test_rays_bitwise_vs_oracle_on_exact_and_inexact_axes(nd, d, og, stepsize):
 
 
 @pytest.mark.parametrize("keys", [-1, 0])
-@pytest.mark.parametrize("warp", [1, 0])
-def test_solve2d_sources_on_the_far_boundaries(keys, warp):
+@pytest.mark.parametrize("kernel", list(KERNELS_2D))
+def test_solve2d_sources_on_the_far_boundaries(keys, kernel):
     """Sources on the bottom and right model edges (where the reference's first
     propagation divides by zero, _fteik2d.py:444-445) next to interior ones,
     in one launch: both comparison paths against the oracle, bit for bit."""
@@ -473,13 +489,11 @@ def test_solve2d_sources_on_the_far_boundaries(keys, warp):
     zmax, xmax = shape[0] * d[0], shape[1] * d[1]
     src = np.array([[zmax, 123.3], [55.5, 100.1], [zmax, xmax], [0.0, 77.7], [133.0, xmax],
                     [zmax, 0.0], [211.1, 150.0]])
-    assert lib.fteik_set_option(b"sweep2d_keys", keys) == 0
-    assert lib.fteik_set_option(b"sweep2d_warp", warp) == 0
+    _set_2d(lib, keys, kernel)
     try:
         tts = fp.Eikonal2D(v, d).solve(src, nsweep=2, return_gradient=True)
     finally:
-        lib.fteik_set_option(b"sweep2d_keys", -1)
-        lib.fteik_set_option(b"sweep2d_warp", -1)
+        _reset_2d(lib)
     tt_o, tg_o, vz_o = O.solve2d(1.0 / v, d, src, 2, True)
     assert bitwise(np.stack([t.grid for t in tts]), tt_o)
     assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)

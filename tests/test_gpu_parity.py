@@ -241,15 +241,6 @@ def test_solve3d_batched_equals_single(nsrc):
     assert bitwise(batch[0].grid, tt_o[0]) and bitwise(batch[-1].grid, tt_o[1])
 
 
-@pytest.mark.parametrize(
-    "shape,d,nsrc,nsweep,seed",
-    [
-        ((24, 32), (10.0, 8.0), 5, 2, 0),
-        ((2, 2), (1.0, 1.0), 2, 2, 1),
-        ((60, 45), (5.0, 7.0), 9, 3, 2),
-        ((13, 90), (10.0, 10.0), 3, 1, 3),
-    ],
-)
 # 2D kernels: (sweep2d_warp, sweep2d_speculate) -- one warp per source with
 # speculated updates (the default for few sources), the same without them,
 # one thread per source
@@ -268,6 +259,15 @@ def _reset_2d(lib):
         lib.fteik_set_option(name, -1)
 
 
+@pytest.mark.parametrize(
+    "shape,d,nsrc,nsweep,seed",
+    [
+        ((24, 32), (10.0, 8.0), 5, 2, 0),
+        ((2, 2), (1.0, 1.0), 2, 2, 1),
+        ((60, 45), (5.0, 7.0), 9, 3, 2),
+        ((13, 90), (10.0, 10.0), 3, 1, 3),
+    ],
+)
 @pytest.mark.parametrize("keys", [-1, 0])
 @pytest.mark.parametrize("kernel", list(KERNELS_2D))
 def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys, kernel):

@@ -230,6 +230,42 @@ __device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, do
   return dle(thr, tev) && dle(thr, ten) && dle(thr, tnv) && dle(thr, tnve);
 }
 
+// The same bound operator by operator, for a node that may change (equal
+// spacings): an operator whose diagonal input (tev, tnv, ten, or tnve for the
+// 3D operator) is >= t0 + 2^-43 M cannot beat t0, so it need not be
+// evaluated, provided leaving it out (its value as Big) keeps the 3D
+// operator's guard max(tv, te, tn) < min(t1d, t2d) as it is: either the
+// guard fails anyway (max(tv, te, tn) >= t1d), or the plane operator's value
+// provably exceeds max(tv, te, tn) (its diagonal input is >= that max +
+// 2^-43 M).  Its value, being >= t0, takes no part in the minimum or the
+// branch record either.  Returns the mask of the plane operators (bit P) and
+// of the 3D operator (bit 3) that may be left out; 0 when the bound does not
+// apply (M tiny, infinite or NaN).
+__device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double tv, double te,
+                                                   double tn, double tev, double ten,
+                                                   double tnv, double tnve) {
+  long long m = __double_as_longlong(t0);
+  m = max(m, __double_as_longlong(tv));
+  m = max(m, __double_as_longlong(te));
+  m = max(m, __double_as_longlong(tn));
+  m = max(m, __double_as_longlong(tev));
+  m = max(m, __double_as_longlong(ten));
+  m = max(m, __double_as_longlong(tnv));
+  m = max(m, __double_as_longlong(tnve));
+  if ((m >> 52) <= 44 || (m >> 52) >= 2047) return 0u;
+  const double eps = __longlong_as_double(m - (43LL << 52));  // 2^-43 M
+  const double thr = t0 + eps;
+  const double mx = dmax(dmax(tv, te), tn);
+  const bool no3d = dle(t1d, mx);
+  const double thr_mx = mx + eps;
+  unsigned dead = 0u;
+  if (dle(thr, tev) && (no3d || dle(thr_mx, tev))) dead |= 1u;
+  if (dle(thr, tnv) && (no3d || dle(thr_mx, tnv))) dead |= 2u;
+  if (dle(thr, ten) && (no3d || dle(thr_mx, ten))) dead |= 4u;
+  if (dle(thr, tnve)) dead |= 8u;
+  return dead;
+}
+
 // Tape entry of a change of node sn (= source * nodes + n) in sweep e: its
 // operator code, and the value t0 it replaced unless this is the node's first
 // change (see Tape3).  A full overflow table flags FTEIK_TAPE_OVERFLOW, which
@@ -766,18 +802,22 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
         }
         if (A.keep_test) go = !keeps_t0(t0, t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve);
       }
+      unsigned dead = 0u;  // operators that provably cannot beat t0 (dead_operators)
       if (go) {
+        if (A.keep_test)
+          dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,
+                                tnve);
         if (COEF) {
-          czx = dlt(tv, te + ca.zxa()) && dlt(te, tv + ca.zxb());
-          czy = dlt(tv, tn + ca.zya()) && dlt(tn, tv + ca.zyb());
-          cxy = dlt(te, tn + ca.xya()) && dlt(tn, te + ca.xyb());
+          czx = !(dead & 1u) && dlt(tv, te + ca.zxa()) && dlt(te, tv + ca.zxb());
+          czy = !(dead & 2u) && dlt(tv, tn + ca.zya()) && dlt(tn, tv + ca.zyb());
+          cxy = !(dead & 4u) && dlt(te, tn + ca.xya()) && dlt(tn, te + ca.xyb());
           if (czx) q_zx = ca.zxq();
           if (czy) q_zy = ca.zyq();
           if (cxy) q_xy = ca.xyq();
         } else {
-          czx = dlt(tv, te + cc.zxa()) && dlt(te, tv + cc.zxb());
-          czy = dlt(tv, tn + cc.zya()) && dlt(tn, tv + cc.zyb());
-          cxy = dlt(te, tn + cc.xya()) && dlt(tn, te + cc.xyb());
+          czx = !(dead & 1u) && dlt(tv, te + cc.zxa()) && dlt(te, tv + cc.zxb());
+          czy = !(dead & 2u) && dlt(tv, tn + cc.zya()) && dlt(tn, tv + cc.zyb());
+          cxy = !(dead & 4u) && dlt(te, tn + cc.xya()) && dlt(tn, te + cc.xyb());
           if (czx) q_zx = cc.zxq();
           if (czy) q_zy = cc.zyq();
           if (cxy) q_xy = cc.xyq();
@@ -828,8 +868,9 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
       const double t2d1 = czx ? sh.r2[warp][0][lane] : kBig;
       const double t2d2 = czy ? sh.r2[warp][1][lane] : kBig;
       const double t2d3 = cxy ? sh.r2[warp][2][lane] : kBig;
-      const bool g3 = go && dlt(dmax(dmax(tv, te), tn),
-                                dmin(dmin(dmin(t1d1, t1d2), t1d3), dmin(dmin(t2d1, t2d2), t2d3)));
+      const bool g3 = go && !(dead & 8u) &&
+                      dlt(dmax(dmax(tv, te), tn),
+                          dmin(dmin(dmin(t1d1, t1d2), t1d3), dmin(dmin(t2d1, t2d2), t2d3)));
       {
         const unsigned m3 = __ballot_sync(0xffffffffu, g3);
         if (g3) {

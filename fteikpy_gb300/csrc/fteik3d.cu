@@ -230,20 +230,29 @@ __device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, do
   return dle(thr, tev) && dle(thr, ten) && dle(thr, tnv) && dle(thr, tnve);
 }
 
-// The same bound operator by operator, for a node that may change (equal
-// spacings): an operator whose diagonal input (tev, tnv, ten, or tnve for the
-// 3D operator) is >= t0 + 2^-43 M cannot beat t0, so it need not be
-// evaluated, provided leaving it out (its value as Big) keeps the 3D
-// operator's guard max(tv, te, tn) < min(t1d, t2d) as it is: either the
-// guard fails anyway (max(tv, te, tn) >= t1d), or the plane operator's value
-// provably exceeds max(tv, te, tn) (its diagonal input is >= that max +
+// Operators that provably cannot beat t0, for a node that may change (equal
+// spacings h).  A plane operator whose guard holds is at least its diagonal
+// input plus h v (v its minimum slowness): with dz2i = dx2i = c its value is
+// diag + sqrt(rad) / 2c (ta + tb = 2 diag, _fteik3d.py:113-117), and the
+// guard |te - tv| < h v bounds (ta - tb)^2 = 4 (te - tv)^2 < 4 h^2 v^2, so
+// rad = 8 c v^2 - c^2 (ta - tb)^2 > 4 c v^2 and sqrt(rad) / 2c > v / sqrt(c)
+// = h v.  Computed in double the value stays within 2^-48 M of that bound, M
+// the largest input (h v included), so an operator with diag + h v (the
+// guard's own coefficient a = h v) >= t0 + 2^-43 M cannot beat t0.  The 3D
+// operator is at least tnve likewise (ta + tb + tc = 3 tnve,
+// _fteik3d.py:149-158).  Such an operator is left out (its value as Big)
+// when that keeps the 3D operator's guard max(tv, te, tn) < min(t1d, t2d) as
+// it is: the guard fails anyway (max(tv, te, tn) >= t1d), or the plane
+// operator provably exceeds max(tv, te, tn) (diag + h v >= that max +
 // 2^-43 M).  Its value, being >= t0, takes no part in the minimum or the
-// branch record either.  Returns the mask of the plane operators (bit P) and
-// of the 3D operator (bit 3) that may be left out; 0 when the bound does not
-// apply (M tiny, infinite or NaN).
+// branch record either.  a_zx, a_zy, a_xy: the planes' guard coefficients.
+// Returns the mask of the plane operators (bit P) and of the 3D operator
+// (bit 3) that may be left out; 0 when the bound does not apply (M tiny,
+// infinite or NaN).
 __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double tv, double te,
                                                    double tn, double tev, double ten,
-                                                   double tnv, double tnve) {
+                                                   double tnv, double tnve, double a_zx,
+                                                   double a_zy, double a_xy) {
   long long m = __double_as_longlong(t0);
   m = max(m, __double_as_longlong(tv));
   m = max(m, __double_as_longlong(te));
@@ -252,16 +261,20 @@ __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double
   m = max(m, __double_as_longlong(ten));
   m = max(m, __double_as_longlong(tnv));
   m = max(m, __double_as_longlong(tnve));
+  m = max(m, __double_as_longlong(a_zx));
+  m = max(m, __double_as_longlong(a_zy));
+  m = max(m, __double_as_longlong(a_xy));
   if ((m >> 52) <= 44 || (m >> 52) >= 2047) return 0u;
   const double eps = __longlong_as_double(m - (43LL << 52));  // 2^-43 M
   const double thr = t0 + eps;
   const double mx = dmax(dmax(tv, te), tn);
   const bool no3d = dle(t1d, mx);
   const double thr_mx = mx + eps;
+  const double b_zx = tev + a_zx, b_zy = tnv + a_zy, b_xy = ten + a_xy;
   unsigned dead = 0u;
-  if (dle(thr, tev) && (no3d || dle(thr_mx, tev))) dead |= 1u;
-  if (dle(thr, tnv) && (no3d || dle(thr_mx, tnv))) dead |= 2u;
-  if (dle(thr, ten) && (no3d || dle(thr_mx, ten))) dead |= 4u;
+  if (dle(thr, b_zx) && (no3d || dle(thr_mx, b_zx))) dead |= 1u;
+  if (dle(thr, b_zy) && (no3d || dle(thr_mx, b_zy))) dead |= 2u;
+  if (dle(thr, b_xy) && (no3d || dle(thr_mx, b_xy))) dead |= 4u;
   if (dle(thr, tnve)) dead |= 8u;
   return dead;
 }
@@ -804,20 +817,34 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
       }
       unsigned dead = 0u;  // operators that provably cannot beat t0 (dead_operators)
       if (go) {
-        if (A.keep_test)
-          dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,
-                                tnve);
+        double a_zx, a_zy, a_xy;
         if (COEF) {
-          czx = !(dead & 1u) && dlt(tv, te + ca.zxa()) && dlt(te, tv + ca.zxb());
-          czy = !(dead & 2u) && dlt(tv, tn + ca.zya()) && dlt(tn, tv + ca.zyb());
-          cxy = !(dead & 4u) && dlt(te, tn + ca.xya()) && dlt(tn, te + ca.xyb());
+          a_zx = ca.zxa();
+          a_zy = ca.zya();
+          a_xy = ca.xya();
+          czx = dlt(tv, te + a_zx) && dlt(te, tv + ca.zxb());
+          czy = dlt(tv, tn + a_zy) && dlt(tn, tv + ca.zyb());
+          cxy = dlt(te, tn + a_xy) && dlt(tn, te + ca.xyb());
+        } else {
+          a_zx = cc.zxa();
+          a_zy = cc.zya();
+          a_xy = cc.xya();
+          czx = dlt(tv, te + a_zx) && dlt(te, tv + cc.zxb());
+          czy = dlt(tv, tn + a_zy) && dlt(tn, tv + cc.zyb());
+          cxy = dlt(te, tn + a_xy) && dlt(tn, te + cc.xyb());
+        }
+        if (A.keep_test) {
+          dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,
+                                tnve, a_zx, a_zy, a_xy);
+          czx = czx && !(dead & 1u);
+          czy = czy && !(dead & 2u);
+          cxy = cxy && !(dead & 4u);
+        }
+        if (COEF) {
           if (czx) q_zx = ca.zxq();
           if (czy) q_zy = ca.zyq();
           if (cxy) q_xy = ca.xyq();
         } else {
-          czx = !(dead & 1u) && dlt(tv, te + cc.zxa()) && dlt(te, tv + cc.zxb());
-          czy = !(dead & 2u) && dlt(tv, tn + cc.zya()) && dlt(tn, tv + cc.zyb());
-          cxy = !(dead & 4u) && dlt(te, tn + cc.xya()) && dlt(tn, te + cc.xyb());
           if (czx) q_zx = cc.zxq();
           if (czy) q_zy = cc.zyq();
           if (cxy) q_xy = cc.xyq();

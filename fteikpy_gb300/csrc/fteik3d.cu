@@ -180,27 +180,6 @@ __device__ __forceinline__ double finish3d(double t0, double t1d1, double t1d2, 
   return tnew;
 }
 
-// One node update, _fteik3d.py:38-200.  Takes the three 1D candidates
-// (_fteik3d.py:76-104: t1d1 = tv + c.z1() ...), which the caller computes
-// first to test whether the node can change.
-template <bool GRAD, class CP>
-__device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
-                                                double te, double tn, double tev, double ten,
-                                                double tnv, double tnve, double t0,
-                                                const CP& c, const Ops3& o, int sz, int sx,
-                                                int sy, uint8_t& code) {
-  const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
-  double t2d1 = kBig, t2d2 = kBig, t2d3 = kBig;
-  if (dlt(tv, te + c.zxa()) && dlt(te, tv + c.zxb())) t2d1 = plane3(0, tv, te, tev, c.zxq(), o);
-  if (dlt(tv, tn + c.zya()) && dlt(tn, tv + c.zyb())) t2d2 = plane3(1, tv, tn, tnv, c.zyq(), o);
-  if (dlt(te, tn + c.xya()) && dlt(tn, te + c.xyb())) t2d3 = plane3(2, te, tn, ten, c.xyq(), o);
-  const double t2d = dmin(dmin(t2d1, t2d2), t2d3);
-  double t3d = kBig;
-  if (dlt(dmax(dmax(tv, te), tn), dmin(t1d, t2d)))
-    t3d = op3d(tv, te, tn, tev, ten, tnv, tnve, c.t3(), o);
-  return finish3d<GRAD>(t0, t1d1, t1d2, t1d3, t2d1, t2d2, t2d3, t3d, sz, sx, sy, code);
-}
-
 // True when the node provably keeps t0 in this sweep, on a grid with equal
 // spacings.  There every plane operator's value is its diagonal input plus a
 // non-negative root term (_fteik3d.py:113-117 with dz2i = dx2i: ta + tb =
@@ -277,6 +256,35 @@ __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double
   if (dle(thr, b_xy) && (no3d || dle(thr_mx, b_xy))) dead |= 4u;
   if (dle(thr, tnve)) dead |= 8u;
   return dead;
+}
+
+// One node update, _fteik3d.py:38-200.  Takes the three 1D candidates
+// (_fteik3d.py:76-104: t1d1 = tv + c.z1() ...), which the caller computes
+// first to test whether the node can change.  With `bounds` (equal
+// spacings), operators that provably cannot beat t0 are left out
+// (dead_operators).
+template <bool GRAD, class CP>
+__device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
+                                                double te, double tn, double tev, double ten,
+                                                double tnv, double tnve, double t0,
+                                                const CP& c, const Ops3& o, int sz, int sx,
+                                                int sy, bool bounds, uint8_t& code) {
+  const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
+  const double a_zx = c.zxa(), a_zy = c.zya(), a_xy = c.xya();
+  const bool gzx = dlt(tv, te + a_zx) && dlt(te, tv + c.zxb());
+  const bool gzy = dlt(tv, tn + a_zy) && dlt(tn, tv + c.zyb());
+  const bool gxy = dlt(te, tn + a_xy) && dlt(tn, te + c.xyb());
+  const unsigned dead =
+      bounds ? dead_operators(t0, t1d, tv, te, tn, tev, ten, tnv, tnve, a_zx, a_zy, a_xy) : 0u;
+  double t2d1 = kBig, t2d2 = kBig, t2d3 = kBig;
+  if (gzx && !(dead & 1u)) t2d1 = plane3(0, tv, te, tev, c.zxq(), o);
+  if (gzy && !(dead & 2u)) t2d2 = plane3(1, tv, tn, tnv, c.zyq(), o);
+  if (gxy && !(dead & 4u)) t2d3 = plane3(2, te, tn, ten, c.xyq(), o);
+  const double t2d = dmin(dmin(t2d1, t2d2), t2d3);
+  double t3d = kBig;
+  if (!(dead & 8u) && dlt(dmax(dmax(tv, te), tn), dmin(t1d, t2d)))
+    t3d = op3d(tv, te, tn, tev, ten, tnv, tnve, c.t3(), o);
+  return finish3d<GRAD>(t0, t1d1, t1d2, t1d3, t2d1, t2d2, t2d3, t3d, sz, sx, sy, code);
 }
 
 // Tape entry of a change of node sn (= source * nodes + n) in sweep e: its
@@ -574,9 +582,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         if (__any_sync(0xffffffffu, go) && go) {
           uint8_t code = 0;
           res = COEF ? node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
-                                           ca, o, sz, sx, sy, code)
+                                           ca, o, sz, sx, sy, keep_test != 0, code)
                      : node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
-                                           cc, o, sz, sx, sy, code);
+                                           cc, o, sz, sx, sy, keep_test != 0, code);
           if (!deq(res, t0)) {
             tts[n] = res;
             if (GRAD) recs[n] = code;

@@ -62,9 +62,10 @@ __device__ __forceinline__ double plane_op(double p, double cp, double q, double
 //    U[a][b][c] indexed upwind-first (a = 0 is the reference's cell row i1 =
 //    i - sgnvz, a = 1 the other row of the pair {max(i-1,0), min(i,nz-2)};
 //    b, c likewise along j, k), which stay in L2 for any number of sources.
-struct CoefArrays {
+template <class I>
+struct CoefArraysT {
   const Coef3& C;
-  long long oz1, ox1, oy1, ozx, ozy, oxy, ot3;
+  I oz1, ox1, oy1, ozx, ozy, oxy, ot3;
   __device__ __forceinline__ double z1() const { return __ldg(C.z1 + oz1); }
   __device__ __forceinline__ double x1() const { return __ldg(C.x1 + ox1); }
   __device__ __forceinline__ double y1() const { return __ldg(C.y1 + oy1); }
@@ -79,6 +80,7 @@ struct CoefArrays {
   __device__ __forceinline__ double xyq() const { return __ldg(C.xyq + oxy); }
   __device__ __forceinline__ double t3() const { return __ldg(C.t3 + ot3); }
 };
+using CoefArrays = CoefArraysT<long long>;
 
 struct CoefCells {
   double U[2][2][2];
@@ -437,7 +439,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       KL = A.order[p] & 0xffff;
     }
     const Ops3& o = *op;
-    const long long NXY = (long long)NX * NY;
+    const int NXY = NX * NY;  // nodes < 2^31 (checked by the host)
     const int dir = e & 7;
     const int sz = dir < 4 ? 1 : -1, sx = (dir & 1) ? -1 : 1, sy = (dir & 2) ? -1 : 1;
     const int J = sx > 0 ? JL : PJ - 1 - JL;
@@ -480,17 +482,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     // Offsets of the coefficient reads that depend on the column only (see
     // Coef3): j1, k1 are the upwind cell indices of the reference.
     const int j1 = sx > 0 ? j - 1 : j, k1 = sy > 0 ? k - 1 : k;
-    const long long jk = (long long)j * NY + k;
-    const long long j1k = (long long)j1 * NY + k, jk1 = (long long)j * NY + k1;
-    const long long j1k1 = (long long)j1 * NY + k1;
+    const int jk = j * NY + k;
+    const int j1k = j1 * NY + k, jk1 = j * NY + k1;
+    const int j1k1 = j1 * NY + k1;
     // Slowness cell offsets around the column, upwind cell first (CoefCells).
     const int jm = imax(j - 1, 0), jp = imin(j, NX - 2);
     const int km = imax(k - 1, 0), kp = imin(k, NY - 2);
-    const long long NYc = ny, NXYc = (long long)nx * ny;
-    const long long ju = (sx > 0 ? jm : jp) * NYc, jo = (sx > 0 ? jp : jm) * NYc;
-    const long long ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
-    const long long dj = (long long)sx * NY, dk = sy;
-    const long long di = (long long)sz * NXY;
+    const int NYc = ny, NXYc = nx * ny;
+    const int ju = (sx > 0 ? jm : jp) * NYc, jo = (sx > 0 ? jp : jm) * NYc;
+    const int ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
+    const int dj = sx * NY, dk = sy;
+    const int di = sz * NXY;
     const bool may_skip = *no_skip == 0;
     const long long big_bits = __double_as_longlong(kBig);
 
@@ -522,7 +524,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       const int r = s - lj - lk;
       const bool act = in_grid && r >= 0 && r < NZ;
       const int i = sz > 0 ? r : NZ - 1 - r;
-      const long long n = (long long)i * NXY + jk;
+      const int n = i * NXY + jk;
       const double t0 = act ? ld_cg(tts + n) : 0.0;
       double res = t0;
       bool upd = act && r != 0 && !frozen_jk;
@@ -550,10 +552,10 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
       if (__any_sync(0xffffffffu, upd)) {
         // Coefficients (see Coef3): read lazily from the arrays, or derived
         // from the 8 slowness cells around the node.
-        const long long i0 = (long long)i * NXY;
-        const long long i1 = (long long)(sz > 0 ? i - 1 : i) * NXY;
-        const CoefArrays ca{C,        i1 + jk,  i0 + j1k,  i0 + jk1,
-                            i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
+        const int i0 = i * NXY;
+        const int i1 = (sz > 0 ? i - 1 : i) * NXY;
+        const CoefArraysT<int> ca{C,        i1 + jk,  i0 + j1k,  i0 + jk1,
+                                  i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
         CoefCells cc{{}, o};
         double t1d1 = 0.0, t1d2 = 0.0, t1d3 = 0.0;
         bool go = upd;
@@ -681,7 +683,7 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
   const unsigned total_items = (unsigned)A.nepochs * per_epoch;
   const unsigned cmask = (unsigned)A.chunk - 1u;
   const Ops3& o = A.o;
-  const long long NXY = (long long)A.NX * A.NY;
+  const int NXY = A.NX * A.NY;  // nodes < 2^31 (checked by the host)
   const int T = A.total_steps;
 
   for (;;) {
@@ -732,18 +734,18 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
     const bool in_grid = j < A.NX && k < A.NY;
     const bool frozen_jk = (j == (sx > 0 ? 0 : A.NX - 1)) || (k == (sy > 0 ? 0 : A.NY - 1));
     const int j1 = sx > 0 ? j - 1 : j, k1 = sy > 0 ? k - 1 : k;
-    const long long jk = (long long)j * A.NY + k;
-    const long long j1k = (long long)j1 * A.NY + k, jk1 = (long long)j * A.NY + k1;
-    const long long j1k1 = (long long)j1 * A.NY + k1;
+    const int jk = j * A.NY + k;
+    const int j1k = j1 * A.NY + k, jk1 = j * A.NY + k1;
+    const int j1k1 = j1 * A.NY + k1;
     const int jm = imax(j - 1, 0), jp = imin(j, A.NX - 2);
     const int km = imax(k - 1, 0), kp = imin(k, A.NY - 2);
-    const long long NYc = A.ny, NXYc = (long long)A.nx * A.ny;
-    const long long ju = (sx > 0 ? jm : jp) * NYc, jo = (sx > 0 ? jp : jm) * NYc;
-    const long long ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
+    const int NYc = A.ny, NXYc = A.nx * A.ny;
+    const int ju = (sx > 0 ? jm : jp) * NYc, jo = (sx > 0 ? jp : jm) * NYc;
+    const int ku = sy > 0 ? km : kp, ko = sy > 0 ? kp : km;
     double* tts = A.tt + (long long)src_c * A.nodes;
     uint8_t* recs = GRAD ? A.rec + (long long)src_c * A.nodes : nullptr;
-    const long long dj = (long long)sx * A.NY, dk = sy;
-    const long long di = (long long)sz * NXY;
+    const int dj = sx * A.NY, dk = sy;
+    const int di = sz * NXY;
     const bool may_skip = *A.no_skip == 0;
     const long long big_bits = __double_as_longlong(kBig);
 
@@ -773,17 +775,17 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
       const int r = s - lj - lk;
       const bool act = active && in_grid && r >= 0 && r < A.NZ;
       const int i = sz > 0 ? r : A.NZ - 1 - r;
-      const long long n = (long long)i * NXY + jk;
+      const int n = i * NXY + jk;
       const double t0 = act ? ld_cg(tts + n) : 0.0;
       double res = t0;
       bool go = act && r != 0 && !frozen_jk;
       double tv = 0.0, te = 0.0, tn = 0.0, tev = 0.0, tnv = 0.0, ten = 0.0, tnve = 0.0;
       double t1d1 = kBig, t1d2 = kBig, t1d3 = kBig;
       bool czx = false, czy = false, cxy = false;
-      const long long i0 = (long long)i * NXY;
-      const long long i1 = (long long)(sz > 0 ? i - 1 : i) * NXY;
-      const CoefArrays ca{A.C,      i1 + jk,  i0 + j1k,  i0 + jk1,
-                          i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
+      const int i0 = i * NXY;
+      const int i1 = (sz > 0 ? i - 1 : i) * NXY;
+      const CoefArraysT<int> ca{A.C,      i1 + jk,  i0 + j1k,  i0 + jk1,
+                                i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
       CoefCells cc{{}, o};
       double q_zx = 0.0, q_zy = 0.0, q_xy = 0.0;
       if (go) {
@@ -1404,6 +1406,11 @@ static int solve3d_impl(const double* slow, int nz, int nx, int ny, double dz, d
   if (nepochs * stride >= (1ull << 31) || nepochs * PJ * PK * (unsigned long long)nsrc >= (1ull << 31) ||
       PJ >= (1 << 15) || PK >= (1 << 16))
     return kInvalidArgument;
+  // the sweep kernels index a model's nodes with 32-bit integers
+  if (nodes >= (1LL << 31)) {
+    set_last_error("a 3D model may hold at most 2^31 - 1 nodes ((nz+1)(nx+1)(ny+1) = %lld)", nodes);
+    return kInvalidArgument;
+  }
 
   char* ws = (char*)workspace;
   const Ops3 o = make_ops3(dz, dx, dy);
@@ -1685,7 +1692,7 @@ static int solve_batch_impl(int nmodel, const double* const* slow, const int* di
       coef += (size_t)kNumCoef * M.nodes;
       epochs_steps_max = std::max(epochs_steps_max, (long long)M.stride);
       max_diag = std::max(max_diag, M.PJ + M.PK - 1);
-      if (M.PJ >= (1 << 15) || M.PK >= (1 << 16)) return kInvalidArgument;
+      if (M.PJ >= (1 << 15) || M.PK >= (1 << 16) || M.nodes >= (1LL << 31)) return kInvalidArgument;
       for (int s = 0; s < nsrc[m]; ++s, ++job) {
         Job3& J = jobs[(size_t)job];
         J.model = m;

@@ -110,6 +110,17 @@ def _solve3d(lib, src, nz=4, nx=5, ny=6, d=(1.0, 1.0, 1.0), ws_bytes=None, nswee
     )
 
 
+def test_models_above_2_31_nodes_are_refused_host_side(lib):
+    """The sweep kernels index a model's nodes with 32-bit integers: a model
+    of 2^31 nodes or more is refused before any device work, with a message."""
+    src = np.zeros((1, 3))
+    rc = lib.fteik3d_solve(FAKE, 1290, 1290, 1290, 1.0, 1.0, 1.0,
+                           src.ctypes.data_as(ctypes.c_void_p), 1, 2, 0, FAKE, FAKE, FAKE, FAKE,
+                           1 << 62, 0, None)
+    assert rc == _lib.INVALID_ARGUMENT
+    assert b"2^31" in lib.fteik_last_error()
+
+
 def test_source_out_of_bound_is_host_side(lib):
     # fteikpy/_fteik/_fteik3d.py:403-407: 0 <= src <= d * n on every axis
     assert _solve3d(lib, [4.0 + 1e-9, 0.0, 0.0]) == _lib.SOURCE_OUT_OF_BOUND

@@ -651,6 +651,53 @@ def fd_check(O, v, src, rec, t_obs, g, ncells, tie_free, min_frac, seed=3):
     }
 
 
+def run_fd_cpu(args):
+    """The finite-difference checks of --config 5 on the host alone: the
+    gradient is the oracle's sequential reverse-mode adjoint, which the GPU
+    gradient equals to about 2e-15 of its largest entry on this problem (the
+    GPU run of --config 5 and tests/test_gpu_configs.py check that on every
+    cell), and the central differences go through the oracle's solve as in
+    --config 5. The GPU's time is not spent on the host's finite differences."""
+    from oracle import oracle as O
+
+    shape = (48, 64, 64) if args.small else (96, 128, 128)
+    v0, vt = tomography_models(shape)
+    src = surface_sources(shape, n_side=4 if args.small else 8, seed=7)
+    rec = surface_receivers(shape, n=NREC, seed=11)
+    t_obs = oracle_receiver_times(O, vt, src, rec)[0]
+
+    def gradient(v):
+        T = oracle_receiver_times(O, v, src, rec)[0]
+        s = 1.0 / v
+        return -O.adjoint3d(s, D, src, NSWEEP, rec, T - t_obs) * s * s
+
+    q0 = time.perf_counter()
+    vb = tie_broken(v0)
+    tie_free = fd_check(O, vb, src, rec, t_obs, gradient(vb), args.fd_cells, True, 1e-2)
+    tie_free["model"] = ("the start model with every cell's velocity times (1 + 1e-3 u), u "
+                         "seeded uniform in [-1, 1]")
+    tie_free["selection"] = ("seeded; |grad| >= 1e-2 max|grad|; no kept operator's slowness "
+                             "minimum has a second cell within 4e-6 of it; the sweeps' "
+                             "decisions (oracle digests) identical at v - h, v, v + h")
+    g0 = gradient(v0)
+    start = fd_check(O, v0, src, rec, t_obs, g0, args.fd_cells, False, 1e-4)
+    _, _, tied0 = oracle_receiver_times(O, v0, src, rec, probe=True, margin=TIE_MARGIN)
+    pool0 = np.flatnonzero(np.abs(g0.ravel()) >= 1e-4 * np.abs(g0).max())
+    start["tie_free_significant_cells"] = int((~tied0.ravel()[pool0]).sum())
+    start["selection"] = "seeded, |grad| >= 1e-4 max|grad| (ties included)"
+    print(json.dumps({
+        "config": 5,
+        "metric": "finite-difference check of d(loss)/d(velocity), %dx%dx%d, %d sources x 400 "
+                  "receivers, nsweep=2" % (shape + (len(src),)),
+        "gradient": "the oracle's reverse-mode adjoint (equal to the GPU gradient to ~2e-15 "
+                    "of its largest entry)",
+        "fd": {"rel_step": FD_STEP, "cells_within_1e-6": tie_free["cells_within_1e-6"],
+               "tie_free": tie_free, "start_model": start},
+        "host_seconds": time.perf_counter() - q0, "threads": os.cpu_count(),
+    }))
+    return 0
+
+
 def run_config5(args):
     """Adjoint gradient for tomography: 96 x 128 x 128 at 10 m, 64 surface
     sources x 400 surface receivers, loss = 0.5 sum((T_pred - T_obs)^2) with
@@ -795,6 +842,9 @@ def main():
                          "(default), 4: uneven multi-model batch, 5: adjoint gradient")
     ap.add_argument("--fd-cells", type=int, default=50,
                     help="cells of the finite-difference check of --config 5")
+    ap.add_argument("--fd-cpu", action="store_true",
+                    help="--config 5: only the finite-difference checks, on the host, with the "
+                         "oracle's adjoint as the gradient")
     ap.add_argument("--adj-shape", default=None,
                     help="--config 5: grid cells nz,nx,ny (default 96,128,128)")
     ap.add_argument("--adj-sources", type=int, default=0,
@@ -821,6 +871,8 @@ def main():
         SHAPE, NSRC = (64, 128, 128), 192
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 5 and args.fd_cpu:
+        return run_fd_cpu(args)
     if args.config in (1, 2, 4, 5):
         import torch
 

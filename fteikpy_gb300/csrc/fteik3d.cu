@@ -659,13 +659,23 @@ __device__ __forceinline__ void team_job(const int (&pre)[kTeamWarps + 1], int q
 }
 
 struct TeamShared {
-  // plane jobs, warp w's in [w][0, n2[w]): plane, lane and inputs (u, w, x, q4)
-  double ju[kTeamWarps][96], jw[kTeamWarps][96], jx[kTeamWarps][96], jq[kTeamWarps][96];
-  int jid[kTeamWarps][96];  // plane * 32 + lane
+  // The plane jobs (written in stage A, read in stage B) and the 3D jobs
+  // (written in stage C, read in stage D) share their memory: a barrier
+  // separates their uses, and the smaller footprint leaves more of the SM's
+  // memory to L1.
+  union {
+    struct {
+      // plane jobs, warp w's in [w][0, n2[w]): plane, lane and inputs (u, w, x, q4)
+      double ju[kTeamWarps][96], jw[kTeamWarps][96], jx[kTeamWarps][96], jq[kTeamWarps][96];
+      int jid[kTeamWarps][96];  // plane * 32 + lane
+    };
+    struct {
+      // 3D jobs: lane and inputs (tv, te, tn, tev, ten, tnv, tnve, t2)
+      double kin[8][kTeamWarps][32];
+      int kid[kTeamWarps][32];
+    };
+  };
   double r2[kTeamWarps][3][32];
-  // 3D jobs: lane and inputs (tv, te, tn, tev, ten, tnv, tnve, t2)
-  double kin[8][kTeamWarps][32];
-  int kid[kTeamWarps][32];
   double r3[kTeamWarps][32];
   int n2[kTeamWarps], n3[kTeamWarps];
   unsigned ticket;

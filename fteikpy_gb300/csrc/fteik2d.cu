@@ -477,27 +477,29 @@ __global__ void __launch_bounds__(32) solve2d_kernel(const double* slow, const d
 // the results are the same bits.
 constexpr int kChunk2 = 128;  // rows per precomputed chunk
 
-struct Pre2 {
-  double a1[kChunk2];    // dz * min slowness along z (t1d1 = tv + a1)
-  double t1d2[kChunk2];  // te + dx * min slowness along x
-  double c1[kChunk2];    // te + dx * vref (guard tv <= c1)
-  double b[kChunk2];     // dz * vref (guard te <= tv + b)
-  double p1[kChunk2];    // tev + te (ta = p1 - tv)
-  double p2[kChunk2];    // tev - te (tb = p2 + tv)
-  double x[kChunk2];     // 4 vref^2 (dz2i + dx2i), the radicand's constant term
-  double te[kChunk2], tev[kChunk2], vref[kChunk2];
-  double vv[kChunk2];    // vref * vref
-  double d3[kChunk2];    // the third operator's guard bound
-  double t2[kChunk2];    // the second operator's value, where it applies
+template <int N>
+struct Pre2T {
+  double a1[N];    // dz * min slowness along z (t1d1 = tv + a1)
+  double t1d2[N];  // te + dx * min slowness along x
+  double c1[N];    // te + dx * vref (guard tv <= c1)
+  double b[N];     // dz * vref (guard te <= tv + b)
+  double p1[N];    // tev + te (ta = p1 - tv)
+  double p2[N];    // tev - te (tb = p2 + tv)
+  double x[N];     // 4 vref^2 (dz2i + dx2i), the radicand's constant term
+  double te[N], tev[N], vref[N];
+  double vv[N];    // vref * vref
+  double d3[N];    // the third operator's guard bound
+  double t2[N];    // the second operator's value, where it applies
   // Speculation: the whole update of the row evaluated with tv equal to the
   // previous node's value before this pass (tvs), giving tns and its branch
   // code cds.  When the previous node keeps its value in the pass (most
   // nodes of most passes), the chain's actual tv has the same bits as tvs
   // and lane 0 takes the result instead of evaluating the operators.
-  double tvs[kChunk2], tns[kChunk2];
-  unsigned char flags[kChunk2];  // 1: tev <= te; 2: the second operator applies
-  unsigned char cds[kChunk2];
+  double tvs[N], tns[N];
+  unsigned char flags[N];  // 1: tev <= te; 2: the second operator applies
+  unsigned char cds[N];
 };
+using Pre2 = Pre2T<kChunk2>;
 
 // The precomputed terms the chain reads on every node, loaded into registers
 // one node ahead (the rarer branches read shared memory directly).
@@ -505,7 +507,8 @@ struct Row2 {
   double a1, t1d2, c1, b, p1, p2, x, te, tev, tvs, tns;
   unsigned flags, cds;
 };
-__device__ __forceinline__ Row2 load_row2(const Pre2& P, int q) {
+template <class PreT>
+__device__ __forceinline__ Row2 load_row2(const PreT& P, int q) {
   return Row2{P.a1[q], P.t1d2[q], P.c1[q], P.b[q],   P.p1[q],    P.p2[q],    P.x[q],
               P.te[q], P.tev[q],  P.tvs[q], P.tns[q], P.flags[q], P.cds[q]};
 }
@@ -513,8 +516,8 @@ __device__ __forceinline__ Row2 load_row2(const Pre2& P, int q) {
 // node_update2d on precomputed row q: only the terms that involve tv.
 // Returns the node's value after the update and, when it changes, its branch
 // code (GRAD).
-template <bool GRAD, bool K>
-__device__ __forceinline__ double eval_node2d(const Ops2& o, const Source2& sp, const Pre2& P,
+template <bool GRAD, bool K, class PreT>
+__device__ __forceinline__ double eval_node2d(const Ops2& o, const Source2& sp, const PreT& P,
                                               const Row2& R, int q, int i, int j, int sgntz,
                                               int sgntx, double tv, double t0, unsigned& code) {
   const double t1d1 = tv + R.a1;
@@ -568,8 +571,8 @@ __device__ __forceinline__ double eval_node2d(const Ops2& o, const Source2& sp, 
   return tnew;
 }
 
-template <bool GRAD, bool K, bool SPEC>
-__device__ __forceinline__ void precompute_row2d(Pre2& P, int q, const double* tt,
+template <bool GRAD, bool K, bool SPEC, class PreT>
+__device__ __forceinline__ void precompute_row2d(PreT& P, int q, const double* tt,
                                                  const double* slow, const Ops2& o,
                                                  const Source2& sp, int i, int j, int sgnvz,
                                                  int sgnvx, int sgntz, int sgntx, int NZ,
@@ -723,6 +726,192 @@ __global__ void __launch_bounds__(32) solve2d_warp_kernel(const double* slow, co
     warp_sweeps2d<GRAD, false, SPEC>(P, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
 }
 
+// A block of 4 warps per source.  In the warp kernel the rows of a pass are
+// precomputed chunk by chunk between stretches of the chain, which on the
+// plain 2D workload puts a fifth of the time on the chain's path.  Here warp
+// 0's lane 0 runs the chain while warps 1-3 precompute the pass's chunks of
+// 32 rows ahead of it into a ring of shared-memory slots, each slot published
+// with a tag (pass, chunk) once written.  A pass starts after a block barrier,
+// when every input of its rows is final (the previous column, and this
+// column's values after the previous pass), so only the first chunk's
+// precompute stays on the chain's path.  The rows' operations are the warp
+// kernel's, so the results are the same bits.
+constexpr int kTeamRows2 = 32;                  // rows per chunk
+constexpr int kTeamSlots2 = 8;                  // chunks in the ring
+constexpr int kTeamWarps2 = 4;                  // the chain's warp and three producers
+constexpr unsigned long long kTeamWaitNs2 = 10000000000ull;  // bound of one wait: 10 s
+using Pre2Ring = Pre2T<kTeamRows2 * kTeamSlots2>;
+
+struct TeamSync2 {
+  unsigned long long ready[kTeamSlots2];  // tag of the chunk each slot holds
+  unsigned long long consumed;            // tag of the last chunk the chain finished
+  int abort;                              // a wait gave up: the block stops
+};
+
+// Tags grow with (pass, chunk): pass from 1, chunk c < 2^26 - 1 (rows < 2^31).
+__device__ __forceinline__ unsigned long long tag2(unsigned long long pass, int c) {
+  return (pass << 26) | (unsigned long long)(c + 1);
+}
+
+// Wait until *p >= want. Gives up (false) when another thread of the block
+// gave up, or after kTeamWaitNs2, marking the block aborted.
+__device__ __forceinline__ bool wait_tag2(const volatile unsigned long long* p,
+                                          unsigned long long want, volatile int* abort) {
+  if (*p >= want) return true;
+  const unsigned long long t0 = globaltimer();
+  for (;;) {
+    __nanosleep(32);
+    if (*p >= want) return true;
+    if (*abort) return false;
+    if (globaltimer() - t0 > kTeamWaitNs2) {
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
+// One pass over column j (rows i0, i0 + sgntz, ..., i1), as warp_pass2d.
+template <bool GRAD, bool K, bool SPEC>
+__device__ __forceinline__ void team_pass2d(Pre2Ring& P, TeamSync2& S, double* tt, uint8_t* rec,
+                                            const double* slow, const Ops2& o,
+                                            const Source2& sp, int j, int i0, int i1, int sgnvz,
+                                            int sgnvx, int sgntz, int sgntx, int NZ, int NX,
+                                            unsigned long long pass, unsigned long long& hits) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int step = sgntz;
+  const int len = (i1 - i0) * step + 1;
+  const int nch = (len + kTeamRows2 - 1) / kTeamRows2;
+  __syncthreads();  // the previous pass is complete
+  if (*(volatile int*)&S.abort) return;
+  if (warp > 0) {
+    for (int c = warp - 1; c < nch; c += kTeamWarps2 - 1) {
+      const int slot = c % kTeamSlots2;
+      bool ok = true;
+      if (c >= kTeamSlots2 && lane == 0)
+        ok = wait_tag2(&S.consumed, tag2(pass, c - kTeamSlots2), &S.abort);
+      if (__shfl_sync(0xffffffffu, ok ? 1 : 0, 0) == 0) return;
+      __threadfence_block();
+      const int r0 = c * kTeamRows2;
+      const int m = imin(kTeamRows2, len - r0);
+      if (lane < m)
+        precompute_row2d<GRAD, K, SPEC>(P, slot * kTeamRows2 + lane, tt, slow, o, sp,
+                                        i0 + (r0 + lane) * step, j, sgnvz, sgnvx, sgntz, sgntx,
+                                        NZ, NX);
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence_block();
+        *(volatile unsigned long long*)&S.ready[slot] = tag2(pass, c);
+      }
+    }
+  } else if (lane == 0) {
+    double tv = tt[(long long)(i0 - sgntz) * NX + j];
+    int i = i0;
+    for (int c = 0; c < nch; ++c) {
+      const int slot = c % kTeamSlots2;
+      if (!wait_tag2(&S.ready[slot], tag2(pass, c), &S.abort)) return;
+      __threadfence_block();
+      const int m = imin(kTeamRows2, len - c * kTeamRows2);
+      const int qb = slot * kTeamRows2;
+      double t0n = tt[(long long)i * NX + j];
+      Row2 rn = load_row2(P, qb);
+      for (int q = qb; q < qb + m; ++q, i += step) {
+        const double t0 = t0n;
+        const Row2 r = rn;
+        if (q + 1 < qb + m) {
+          t0n = tt[(long long)(i + step) * NX + j];
+          rn = load_row2(P, q + 1);
+        }
+        unsigned code;
+        double tnew;
+        if (SPEC && deq(tv, r.tvs)) {
+          tnew = r.tns;
+          code = r.cds;
+          ++hits;
+        } else {
+          tnew = eval_node2d<GRAD, K>(o, sp, P, r, q, i, j, sgntz, sgntx, tv, t0, code);
+        }
+        if (!eq2<K>(tnew, t0)) {
+          const long long n = (long long)i * NX + j;
+          tt[n] = tnew;
+          if (GRAD) rec[n] = (uint8_t)code;
+        }
+        tv = tnew;
+      }
+      __threadfence_block();
+      *(volatile unsigned long long*)&S.consumed = tag2(pass, c);
+    }
+  }
+}
+
+template <bool GRAD, bool K, bool SPEC>
+__device__ __noinline__ void team_sweeps2d(Pre2Ring& P, TeamSync2& S, double* tt, uint8_t* rec,
+                                           const double* slow, const Ops2& o, const Source2& sp,
+                                           int nsweep, int NZ, int NX, unsigned long long* stats) {
+  unsigned long long hits = 0, pass = 0;
+  for (int sw = 0; sw < nsweep; ++sw) {
+    for (int j = 1; j < NX; ++j) {
+      team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX,
+                                 ++pass, hits);
+      team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX,
+                                 ++pass, hits);
+    }
+    for (int j = NX - 2; j >= 0; --j) {
+      team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX,
+                                 ++pass, hits);
+      team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX,
+                                 ++pass, hits);
+    }
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(stats, (unsigned long long)nsweep * 4ull * (unsigned long long)(NZ - 1) * (NX - 1));
+    atomicAdd(stats + 1, hits);
+  }
+}
+
+// A block of kTeamWarps2 warps per source (blockIdx.x): thread 0 runs the
+// first propagation, the block checks it for non-finite values, then the
+// sweeps run as above.
+template <bool GRAD, bool SPEC>
+__global__ void __launch_bounds__(kTeamWarps2 * 32)
+    solve2d_team_kernel(const double* slow, const double* src, int nz, int nx, int nsweep,
+                        Ops2 o, double* tt_all, uint8_t* rec_all, Source2* params,
+                        double* vzero_out, bool keys, unsigned long long* stats, int* status) {
+  __shared__ Pre2Ring P;
+  __shared__ TeamSync2 S;
+  __shared__ Source2 sps;
+  const int s = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int NZ = nz + 1, NX = nx + 1;
+  const long long nodes = (long long)NZ * NX;
+  double* tt = tt_all + (long long)s * nodes;
+  uint8_t* rec = GRAD ? rec_all + (long long)s * nodes : nullptr;
+  if (tid == 0) {
+    const Source2 sp = first_propagation2d<GRAD>(slow, src + 2 * s, nz, nx, o, tt, rec);
+    params[s] = sp;
+    vzero_out[s] = sp.vzero;
+    sps = sp;
+    S.consumed = 0;
+    S.abort = 0;
+  }
+  if (tid < kTeamSlots2) S.ready[tid] = 0;
+  __syncthreads();
+  const Source2 sp = sps;
+  bool finite = true;
+  for (int jj = tid; jj < NX; jj += blockDim.x)
+    for (int r = sp.zsi; r <= imin(sp.zsi + 1, NZ - 1); ++r)
+      finite = finite && is_finite(tt[(long long)r * NX + jj]);
+  for (int ii = tid; ii < NZ; ii += blockDim.x)
+    for (int c = sp.xsi; c <= imin(sp.xsi + 1, NX - 1); ++c)
+      finite = finite && is_finite(tt[(long long)ii * NX + c]);
+  finite = __syncthreads_and(finite ? 1 : 0) != 0 && keys;
+  if (finite)
+    team_sweeps2d<GRAD, true, SPEC>(P, S, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
+  else
+    team_sweeps2d<GRAD, false, SPEC>(P, S, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
+  __syncthreads();
+  if (tid == 0 && *(volatile int*)&S.abort) atomicCAS(status, 0, (int)kDeviceWaitTimeout);
+}
+
 __global__ void fill2d_kernel(double* tt, uint8_t* rec, long long n) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
@@ -824,10 +1013,23 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
   // itself (its FP64 pipe is what the chain waits on); beyond that, one
   // thread per source, where each warp instruction serves 32 chains.
   const long long warp_opt = option_value(kOptSweep2dWarp);
-  const bool per_warp = warp_opt >= 0 ? warp_opt != 0 : nsrc <= 4 * sm_count();
+  const int mode = warp_opt >= 0 ? (int)warp_opt
+                                 : (nsrc <= sm_count() ? 2 : (nsrc <= 4 * sm_count() ? 1 : 0));
   const bool spec = option_value(kOptSweep2dSpec) != 0;
   unsigned long long* stats = (unsigned long long*)(ws + L.status + 8);
-  if (per_warp) {
+  if (mode == 2) {
+    // a block per source while every source has an SM to itself
+    int* status = (int*)(ws + L.status);
+#define FTEIK_T2(G, S)                                                                   \
+  solve2d_team_kernel<G, S><<<nsrc, kTeamWarps2 * 32, 0, st>>>(                          \
+      slow, src_dev, nz, nx, nsweep, o, tt, rec, params, vzero, keys, stats, status)
+    if (grad) {
+      if (spec) FTEIK_T2(true, true); else FTEIK_T2(true, false);
+    } else {
+      if (spec) FTEIK_T2(false, true); else FTEIK_T2(false, false);
+    }
+#undef FTEIK_T2
+  } else if (mode == 1) {
 #define FTEIK_W2(G, S)                                                                  \
   solve2d_warp_kernel<G, S><<<nsrc, 32, 0, st>>>(slow, src_dev, nz, nx, nsweep, o, tt, rec, \
                                                  params, vzero, keys, stats)

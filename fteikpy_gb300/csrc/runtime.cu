@@ -117,7 +117,8 @@ extern "C" int fteik_set_option(const char* name, long long value) {
     return kOk;
   }
   if (std::strcmp(name, "sweep2d_warp") == 0) {
-    g_options[kOptSweep2dWarp] = value < 0 ? -1 : (value ? 1 : 0);
+    if (value > 2) return kInvalidArgument;
+    g_options[kOptSweep2dWarp] = value < 0 ? -1 : value;
     return kOk;
   }
   if (std::strcmp(name, "sweep2d_keys") == 0) {

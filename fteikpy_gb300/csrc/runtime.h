@@ -40,7 +40,7 @@ enum Option : int {
   kOptSweepTeam = 4,    // 3D team kernel (compacted operators): 1 on, 0 off
   kOptAdjointChunk = 5, // adjoint reverse sweeps: steps between progress publications
   kOptSweep2dKeys = 6,  // 2D sweeps: 0 forces IEEE comparisons (else integer keys when exact)
-  kOptSweep2dWarp = 7,  // 2D sweeps: 1 one warp per source, 0 one thread per source
+  kOptSweep2dWarp = 7,  // 2D sweeps: 2 a block per source, 1 a warp, 0 one thread
   kOptSweep2dSpec = 8,  // 2D warp sweeps: 0 turns off the speculated updates (same results)
   kOptCount = 9,
 };

@@ -58,7 +58,10 @@ int fteik_kernel_timing(int on);
  * first propagation left only finite values, where the two agree).
  * "sweep2d_warp": 1 runs each 2D source on a warp (the warp precomputes the
  * terms of each column that do not depend on the previous node, one lane
- * runs the chain; the default up to 4 sources per SM), 0 on one thread.
+ * runs the chain; the default up to 4 sources per SM), 0 on one thread, 2
+ * on a block of 4 warps (one lane runs the chain while three warps
+ * precompute the pass's rows ahead of it; the default up to one source per
+ * SM).
  * "sweep2d_speculate": 0 turns off the warp kernel's speculated updates (each
  * row also evaluated with the previous node's value from before the pass,
  * taken when the chain's actual value has the same bits).

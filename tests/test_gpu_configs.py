@@ -60,9 +60,9 @@ def test_config1_plain_2d_both_kernels_and_analytic():
     v, v0, src, d = bench.config1_models()
     ref = O.solve2d(1.0 / v, d, [src], 2, False)[0][0]
     try:
-        # one warp per source with and without speculated updates, one thread
-        # per source; integer-key and IEEE comparisons
-        for warp, spec in ((1, -1), (1, 0), (0, -1)):
+        # a block and a warp per source, each with and without speculated
+        # updates, one thread per source; integer-key and IEEE comparisons
+        for warp, spec in ((2, -1), (2, 0), (1, -1), (1, 0), (0, -1)):
             for keys in (-1, 0):
                 assert lib.fteik_set_option(b"sweep2d_warp", warp) == _lib.OK
                 assert lib.fteik_set_option(b"sweep2d_speculate", spec) == _lib.OK

@@ -241,10 +241,11 @@ def test_solve3d_batched_equals_single(nsrc):
     assert bitwise(batch[0].grid, tt_o[0]) and bitwise(batch[-1].grid, tt_o[1])
 
 
-# 2D kernels: (sweep2d_warp, sweep2d_speculate) -- one warp per source with
-# speculated updates (the default for few sources), the same without them,
-# one thread per source
-KERNELS_2D = {"warp": (1, -1), "warp_nospec": (1, 0), "thread": (0, -1)}
+# 2D kernels: (sweep2d_warp, sweep2d_speculate) -- a block per source with
+# speculated updates (the default up to one source per SM), the same without
+# them, one warp per source with and without them, one thread per source
+KERNELS_2D = {"team": (2, -1), "team_nospec": (2, 0), "warp": (1, -1), "warp_nospec": (1, 0),
+              "thread": (0, -1)}
 
 
 def _set_2d(lib, keys, kernel):
@@ -271,9 +272,10 @@ def _reset_2d(lib):
 @pytest.mark.parametrize("keys", [-1, 0])
 @pytest.mark.parametrize("kernel", list(KERNELS_2D))
 def test_solve2d_bitwise_vs_oracle(shape, d, nsrc, nsweep, seed, keys, kernel):
-    """Both 2D kernels (one warp per source with the rows' tv-independent terms
-    precomputed by the warp, with and without the speculated updates, the
-    default for few sources; one thread per source) and both comparison paths
+    """Every 2D kernel (a block per source whose producer warps precompute the
+    rows' tv-independent terms ahead of the chain, and one warp per source that
+    precomputes them between stretches of it, each with and without the
+    speculated updates; one thread per source) and both comparison paths
     (integer keys, the default for sources whose first propagation is finite;
     IEEE comparisons) against the oracle, bit for bit."""
     from fteikpy_gb300 import _lib

@@ -292,7 +292,7 @@ def test_tuning_options_host_side(lib):
                             (b"sweep_team", (0, 1), ()),
                             (b"adjoint_chunk", (1, 4, 64), (3, 0, 128)),
                             (b"sweep2d_keys", (0, 1), ()),
-                            (b"sweep2d_warp", (0, 1), ()),
+                            (b"sweep2d_warp", (0, 1, 2), (3,)),
                             (b"sweep2d_speculate", (0, 1), ())):
         for g in good:
             assert lib.fteik_set_option(name, g) == 0

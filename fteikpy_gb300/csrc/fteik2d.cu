@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(32) solve2d_warp_kernel(const double* slow, co
 constexpr int kTeamRows2 = 32;                  // rows per chunk
 constexpr int kTeamSlots2 = 8;                  // chunks in the ring
 constexpr int kTeamWarps2 = 4;                  // the chain's warp and three producers
-constexpr unsigned long long kTeamWaitNs2 = 10000000000ull;  // bound of one wait: 10 s
+constexpr unsigned long long kTeamWaitNs2 = 10000000000ull;  // default bound of one wait: 10 s
 using Pre2Ring = Pre2T<kTeamRows2 * kTeamSlots2>;
 
 struct TeamSync2 {
@@ -754,16 +754,17 @@ __device__ __forceinline__ unsigned long long tag2(unsigned long long pass, int 
 }
 
 // Wait until *p >= want. Gives up (false) when another thread of the block
-// gave up, or after kTeamWaitNs2, marking the block aborted.
+// gave up, or after limit_ns, marking the block aborted.
 __device__ __forceinline__ bool wait_tag2(const volatile unsigned long long* p,
-                                          unsigned long long want, volatile int* abort) {
+                                          unsigned long long want, volatile int* abort,
+                                          unsigned long long limit_ns) {
   if (*p >= want) return true;
   const unsigned long long t0 = globaltimer();
   for (;;) {
     __nanosleep(32);
     if (*p >= want) return true;
     if (*abort) return false;
-    if (globaltimer() - t0 > kTeamWaitNs2) {
+    if (globaltimer() - t0 >= limit_ns) {
       *abort = 1;
       return false;
     }
@@ -776,7 +777,8 @@ __device__ __forceinline__ void team_pass2d(Pre2Ring& P, TeamSync2& S, double* t
                                             const double* slow, const Ops2& o,
                                             const Source2& sp, int j, int i0, int i1, int sgnvz,
                                             int sgnvx, int sgntz, int sgntx, int NZ, int NX,
-                                            unsigned long long pass, unsigned long long& hits) {
+                                            unsigned long long pass, unsigned long long wait_ns,
+                                            unsigned long long& hits) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int step = sgntz;
   const int len = (i1 - i0) * step + 1;
@@ -788,7 +790,7 @@ __device__ __forceinline__ void team_pass2d(Pre2Ring& P, TeamSync2& S, double* t
       const int slot = c % kTeamSlots2;
       bool ok = true;
       if (c >= kTeamSlots2 && lane == 0)
-        ok = wait_tag2(&S.consumed, tag2(pass, c - kTeamSlots2), &S.abort);
+        ok = wait_tag2(&S.consumed, tag2(pass, c - kTeamSlots2), &S.abort, wait_ns);
       if (__shfl_sync(0xffffffffu, ok ? 1 : 0, 0) == 0) return;
       __threadfence_block();
       const int r0 = c * kTeamRows2;
@@ -808,7 +810,7 @@ __device__ __forceinline__ void team_pass2d(Pre2Ring& P, TeamSync2& S, double* t
     int i = i0;
     for (int c = 0; c < nch; ++c) {
       const int slot = c % kTeamSlots2;
-      if (!wait_tag2(&S.ready[slot], tag2(pass, c), &S.abort)) return;
+      if (!wait_tag2(&S.ready[slot], tag2(pass, c), &S.abort, wait_ns)) return;
       __threadfence_block();
       const int m = imin(kTeamRows2, len - c * kTeamRows2);
       const int qb = slot * kTeamRows2;
@@ -846,20 +848,21 @@ __device__ __forceinline__ void team_pass2d(Pre2Ring& P, TeamSync2& S, double* t
 template <bool GRAD, bool K, bool SPEC>
 __device__ __noinline__ void team_sweeps2d(Pre2Ring& P, TeamSync2& S, double* tt, uint8_t* rec,
                                            const double* slow, const Ops2& o, const Source2& sp,
-                                           int nsweep, int NZ, int NX, unsigned long long* stats) {
+                                           int nsweep, int NZ, int NX, unsigned long long wait_ns,
+                                           unsigned long long* stats) {
   unsigned long long hits = 0, pass = 0;
   for (int sw = 0; sw < nsweep; ++sw) {
     for (int j = 1; j < NX; ++j) {
       team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 1, 1, 1, NZ, NX,
-                                 ++pass, hits);
+                                 ++pass, wait_ns, hits);
       team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 1, -1, 1, NZ, NX,
-                                 ++pass, hits);
+                                 ++pass, wait_ns, hits);
     }
     for (int j = NX - 2; j >= 0; --j) {
       team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, 1, NZ - 1, 1, 0, 1, -1, NZ, NX,
-                                 ++pass, hits);
+                                 ++pass, wait_ns, hits);
       team_pass2d<GRAD, K, SPEC>(P, S, tt, rec, slow, o, sp, j, NZ - 2, 0, 0, 0, -1, -1, NZ, NX,
-                                 ++pass, hits);
+                                 ++pass, wait_ns, hits);
     }
   }
   if (threadIdx.x == 0) {
@@ -875,7 +878,8 @@ template <bool GRAD, bool SPEC>
 __global__ void __launch_bounds__(kTeamWarps2 * 32)
     solve2d_team_kernel(const double* slow, const double* src, int nz, int nx, int nsweep,
                         Ops2 o, double* tt_all, uint8_t* rec_all, Source2* params,
-                        double* vzero_out, bool keys, unsigned long long* stats, int* status) {
+                        double* vzero_out, bool keys, unsigned long long wait_ns,
+                        unsigned long long* stats, int* status) {
   __shared__ Pre2Ring P;
   __shared__ TeamSync2 S;
   __shared__ Source2 sps;
@@ -905,9 +909,9 @@ __global__ void __launch_bounds__(kTeamWarps2 * 32)
       finite = finite && is_finite(tt[(long long)ii * NX + c]);
   finite = __syncthreads_and(finite ? 1 : 0) != 0 && keys;
   if (finite)
-    team_sweeps2d<GRAD, true, SPEC>(P, S, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
+    team_sweeps2d<GRAD, true, SPEC>(P, S, tt, rec, slow, o, sp, nsweep, NZ, NX, wait_ns, stats);
   else
-    team_sweeps2d<GRAD, false, SPEC>(P, S, tt, rec, slow, o, sp, nsweep, NZ, NX, stats);
+    team_sweeps2d<GRAD, false, SPEC>(P, S, tt, rec, slow, o, sp, nsweep, NZ, NX, wait_ns, stats);
   __syncthreads();
   if (tid == 0 && *(volatile int*)&S.abort) atomicCAS(status, 0, (int)kDeviceWaitTimeout);
 }
@@ -1020,9 +1024,11 @@ extern "C" int fteik2d_solve(const double* slow, int nz, int nx, double dz, doub
   if (mode == 2) {
     // a block per source while every source has an SM to itself
     int* status = (int*)(ws + L.status);
+    const long long wopt = option_value(kOptSweep2dWaitNs);
+    const unsigned long long wait_ns = wopt >= 0 ? (unsigned long long)wopt : kTeamWaitNs2;
 #define FTEIK_T2(G, S)                                                                   \
   solve2d_team_kernel<G, S><<<nsrc, kTeamWarps2 * 32, 0, st>>>(                          \
-      slow, src_dev, nz, nx, nsweep, o, tt, rec, params, vzero, keys, stats, status)
+      slow, src_dev, nz, nx, nsweep, o, tt, rec, params, vzero, keys, wait_ns, stats, status)
     if (grad) {
       if (spec) FTEIK_T2(true, true); else FTEIK_T2(true, false);
     } else {

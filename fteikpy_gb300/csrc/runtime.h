@@ -42,7 +42,8 @@ enum Option : int {
   kOptSweep2dKeys = 6,  // 2D sweeps: 0 forces IEEE comparisons (else integer keys when exact)
   kOptSweep2dWarp = 7,  // 2D sweeps: 2 a block per source, 1 a warp, 0 one thread
   kOptSweep2dSpec = 8,  // 2D warp sweeps: 0 turns off the speculated updates (same results)
-  kOptCount = 9,
+  kOptSweep2dWaitNs = 9,  // 2D block sweeps: bound of one wait between warps, in ns
+  kOptCount = 10,
 };
 long long option_value(int opt);
 

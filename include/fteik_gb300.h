@@ -65,6 +65,9 @@ int fteik_kernel_timing(int on);
  * "sweep2d_speculate": 0 turns off the warp kernel's speculated updates (each
  * row also evaluated with the previous node's value from before the pass,
  * taken when the chain's actual value has the same bits).
+ * "sweep2d_wait_ns": the bound, in ns, of each wait between the warps of the
+ * block-per-source 2D kernel (default 10 s); a wait that reaches it stops
+ * the block and the solve returns FTEIK_DEVICE_WAIT_TIMEOUT.
  * Results are identical for every setting.
  * fteik_get_option reads a knob back. */
 int fteik_set_option(const char* name, long long value);

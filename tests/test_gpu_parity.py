@@ -499,3 +499,32 @@ def test_solve2d_sources_on_the_far_boundaries(keys, kernel):
     tt_o, tg_o, vz_o = O.solve2d(1.0 / v, d, src, 2, True)
     assert bitwise(np.stack([t.grid for t in tts]), tt_o)
     assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)
+
+
+def test_solve2d_block_kernel_wait_gives_up_then_recovers():
+    """The waits between the warps of the block-per-source 2D kernel are
+    bounded. With the bound at 0 ns the chain's first wait for a precomputed
+    chunk gives up, the block stops, and the solve reports the device-side
+    timeout (the reference-facing RuntimeError). The next solve, with the
+    default bound, equals the oracle bit for bit."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    shape, d = (70, 50), (10.0, 10.0)
+    v = 1500.0 + 20.0 * np.arange(shape[0])[:, None] * np.ones(shape)
+    v *= 1.0 + 0.05 * rng.uniform(-1.0, 1.0, shape)
+    src = np.array([[35.5, 260.2], [401.0, 77.3]])
+    assert lib.fteik_set_option(b"sweep2d_warp", 2) == 0
+    try:
+        assert lib.fteik_set_option(b"sweep2d_wait_ns", 0) == 0
+        with pytest.raises(RuntimeError, match="timed out"):
+            fp.Eikonal2D(v, d).solve(src, nsweep=2)
+        assert lib.fteik_set_option(b"sweep2d_wait_ns", -1) == 0
+        tts = fp.Eikonal2D(v, d).solve(src, nsweep=2, return_gradient=True)
+    finally:
+        lib.fteik_set_option(b"sweep2d_wait_ns", -1)
+        lib.fteik_set_option(b"sweep2d_warp", -1)
+    tt_o, tg_o, _ = O.solve2d(1.0 / v, d, src, 2, True)
+    assert bitwise(np.stack([t.grid for t in tts]), tt_o)
+    assert bitwise(np.stack([t._gradient.cpu().numpy() for t in tts]), tg_o)

@@ -53,7 +53,7 @@ BYTES_PER_UPDATE = 25  # slowness + tt read + tt write (8 B each) + 1 B branch r
 # bytes read + written. The bench scales both by the updates of the timed
 # launch.
 TEAM_FP64_LANE_OPS_PER_UPDATE = (63425382894 + 19140040728 + 17058753336) / 3221225472
-TEAM_DRAM_BYTES_PER_UPDATE = (88354825216 + 10732071936) / 3221225472
+TEAM_DRAM_BYTES_PER_UPDATE = (86492250624 + 9309593088) / 3221225472
 
 
 def smooth2d(rng, shape, sigma):

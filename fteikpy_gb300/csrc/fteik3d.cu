@@ -265,6 +265,18 @@ __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double
 // first to test whether the node can change.  With `bounds` (equal
 // spacings), operators that provably cannot beat t0 are left out
 // (dead_operators).
+// A plane operator's guard u < v + a && v < u + b (_fteik3d.py:110,122,134:
+// u, v the two face neighbours, a, b >= 0 the guard's spacing-times-slowness
+// factors) with one addition instead of two.  The clause whose left operand
+// is the smaller holds by itself, as RN(w + c) >= w for c >= 0; with u == v
+// both hold exactly when u < RN(u + min(a, b)), RN(u + .) being monotone.
+__device__ __forceinline__ bool plane_guard(double u, double v, double a, double b) {
+  const bool ul = dlt(u, v), vl = dlt(v, u);
+  const double lo = ul ? u : v, hi = ul ? v : u;
+  const double c = ul ? b : (vl ? a : dmin(a, b));
+  return dlt(hi, lo + c);
+}
+
 template <bool GRAD, class CP>
 __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
                                                 double te, double tn, double tev, double ten,
@@ -273,9 +285,9 @@ __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double
                                                 int sy, bool bounds, uint8_t& code) {
   const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
   const double a_zx = c.zxa(), a_zy = c.zya(), a_xy = c.xya();
-  const bool gzx = dlt(tv, te + a_zx) && dlt(te, tv + c.zxb());
-  const bool gzy = dlt(tv, tn + a_zy) && dlt(tn, tv + c.zyb());
-  const bool gxy = dlt(te, tn + a_xy) && dlt(tn, te + c.xyb());
+  const bool gzx = plane_guard(tv, te, a_zx, c.zxb());
+  const bool gzy = plane_guard(tv, tn, a_zy, c.zyb());
+  const bool gxy = plane_guard(te, tn, a_xy, c.xyb());
   const unsigned dead =
       bounds ? dead_operators(t0, t1d, tv, te, tn, tev, ten, tnv, tnve, a_zx, a_zy, a_xy) : 0u;
   double t2d1 = kBig, t2d2 = kBig, t2d3 = kBig;
@@ -842,16 +854,16 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
           a_zx = ca.zxa();
           a_zy = ca.zya();
           a_xy = ca.xya();
-          czx = dlt(tv, te + a_zx) && dlt(te, tv + ca.zxb());
-          czy = dlt(tv, tn + a_zy) && dlt(tn, tv + ca.zyb());
-          cxy = dlt(te, tn + a_xy) && dlt(tn, te + ca.xyb());
+          czx = plane_guard(tv, te, a_zx, ca.zxb());
+          czy = plane_guard(tv, tn, a_zy, ca.zyb());
+          cxy = plane_guard(te, tn, a_xy, ca.xyb());
         } else {
           a_zx = cc.zxa();
           a_zy = cc.zya();
           a_xy = cc.xya();
-          czx = dlt(tv, te + a_zx) && dlt(te, tv + cc.zxb());
-          czy = dlt(tv, tn + a_zy) && dlt(tn, tv + cc.zyb());
-          cxy = dlt(te, tn + a_xy) && dlt(tn, te + cc.xyb());
+          czx = plane_guard(tv, te, a_zx, cc.zxb());
+          czy = plane_guard(tv, tn, a_zy, cc.zyb());
+          cxy = plane_guard(te, tn, a_xy, cc.xyb());
         }
         if (A.keep_test) {
           dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,

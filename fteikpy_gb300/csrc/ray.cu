@@ -636,6 +636,145 @@ __global__ void ray_axis_kernel(Axes ax, const double* ttgrad, long long gstride
   }
 }
 
+// One warp per ray, for launches of at most one ray per SM sub-partition
+// (one source's receivers), where a step's time is its chain of FP64
+// instructions.  Lane q < ND owns axis q as in ray_axis_kernel.  The blend's
+// weights and products, which the axis kernel repeats on each of a ray's
+// lanes, are spread over the warp: lane NC c + t computes corner t's weight
+// and its product with gradient component c's corner value.  Each sum stays
+// sequential, in the reference's order, on its component's lane, and the
+// squared norm takes each lane's square.  Every value is the same IEEE
+// operation on the same operands as in ray_kernel, so the rays are the same
+// bits, with about a third fewer FP64 instructions per step.
+template <int ND>
+__global__ void __launch_bounds__(128)
+    ray_warp_kernel(Axes ax, const double* ttgrad, long long gstride, const int* gidx,
+                    const double* ends, int nrays, const double* sources, double stepsize,
+                    double dist_min, int max_step, double* rays, int* counts, int* status) {
+  constexpr int NC = 1 << ND;  // corners of a cell
+  __shared__ RayShared S;
+  ray_setup<ND>(ax, S);
+  const int lane = threadIdx.x & 31;
+  const int r = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+  if (r >= nrays) return;
+  const unsigned full = 0xffffffffu, all_axes = (1u << ND) - 1u;
+  const int q = lane < ND ? lane : ND - 1;          // this lane's axis and component
+  const int t = lane & (NC - 1);                    // corner of this lane's product
+  const int pc = lane / NC < ND ? lane / NC : ND - 1;  // component of this lane's product
+  const int gi = gidx ? gidx[r] : 0;
+  const double* g = ttgrad + (long long)gi * gstride;
+  const double* a = q == 0 ? ax.a[0] : (q == 1 ? ax.a[1] : ax.a[ND - 1]);
+  const int n = q == 0 ? ax.n[0] : (q == 1 ? ax.n[1] : ax.n[ND - 1]);
+  const RayAxis& X = S.X[q];
+  const double sq = sources[ND * gi + q];
+  double p = ends[ND * r + q];
+  const long long kmin = __double_as_longlong(dist_min);
+  if (lane == 0) counts[r] = 0;
+  if ((__ballot_sync(full, X.lo <= p && p <= X.hi) & all_axes) != all_axes) {
+    if (lane == 0) status[r] = kEndPointOutOfBound;
+    return;
+  }
+  long long kp = zkey(p);
+  double* ray = rays + (long long)r * max_step * ND;
+  int count = 1;
+  if (lane < ND) ray[q] = p;
+  const long long max_iter = 64LL * max_step + 4096;
+  for (long long iter = 0;; ++iter) {
+    if (iter >= max_iter) {
+      if (lane == 0) status[r] = kMaxStepReached;
+      return;
+    }
+    // dist(src, pcur) >= stepsize on the squared distance (a*a + b*b) + c*c
+    const double dq = sq - p;
+    const double s2 = dq * dq;
+    double dsq = __shfl_sync(full, s2, 0) + __shfl_sync(full, s2, 1);
+    if (ND == 3) dsq = dsq + __shfl_sync(full, s2, 2);
+    const long long db = __double_as_longlong(dsq);
+    if (db < kmin || db > 0x7ff0000000000000LL) break;
+    if ((__ballot_sync(full, X.klo <= kp && kp <= X.khi) & all_axes) != all_axes) break;
+    // this lane's axis: cell, corner coordinates, weight differences
+    const int c = ray_search(a, n, X, p, kp);
+    const bool e = c == n - 1;
+    const double x1 = __ldg(a + c);
+    const double x2 = e ? 2.0 * x1 - __ldg(a + n - 2) : __ldg(a + c + 1);
+    const double lo = x1 - p, hi = x2 - p, span = x2 - x1;
+    double L[ND], H[ND];
+    int ci[ND];
+    bool ce[ND];
+#pragma unroll
+    for (int u = 0; u < ND; ++u) {
+      L[u] = __shfl_sync(full, lo, u);
+      H[u] = __shfl_sync(full, hi, u);
+      const int packed = __shfl_sync(full, (c << 1) | (e ? 1 : 0), u);
+      ci[u] = packed >> 1;
+      ce[u] = (packed & 1) != 0;
+    }
+    double vol = S.vol_c;
+    if (!S.uni) {
+      vol = __shfl_sync(full, span, 0) * __shfl_sync(full, span, 1);
+      if (ND == 3) vol = vol * __shfl_sync(full, span, 2);
+      vol = fabs(vol);
+    }
+    // corner t's weight (weights3 / weights2: |(x? - xq)(y? - yq)(z? - zq)|)
+    // and its product with component pc's value there (1.0 past the last node)
+    double w, cv;
+    if (ND == 3) {
+      const double pair = ((t & 1) ? L[0] : H[0]) * ((t & 2) ? L[1] : H[1]);
+      w = fabs(pair * ((t & 4) ? L[ND - 1] : H[ND - 1]));
+      const int n1 = ax.n[1], n2 = ax.n[ND - 1];
+      const long long b = ((long long)ci[0] * n1 + ci[1]) * n2 + ci[ND - 1];
+      const long long off =
+          ((t & 1) ? (long long)n1 * n2 : 0) + ((t & 2) ? n2 : 0) + ((t & 4) ? 1 : 0);
+      const bool past = ((t & 1) && ce[0]) || ((t & 2) && ce[1]) || ((t & 4) && ce[ND - 1]);
+      cv = past ? 1.0 : __ldg(g + (b + off) * 3 + pc);
+    } else {
+      w = fabs(((t & 1) ? L[0] : H[0]) * ((t & 2) ? L[1] : H[1]));
+      const int n1 = ax.n[1];
+      const long long b = (long long)ci[0] * n1 + ci[1];
+      const long long off = ((t & 1) ? n1 : 0) + ((t & 2) ? 1 : 0);
+      const bool past = ((t & 1) && ce[0]) || ((t & 2) && ce[1]);
+      cv = past ? 1.0 : __ldg(g + (b + off) * 2 + pc);
+    }
+    const double prod = cv * w;
+    // component q's blend, in the reference's order
+    double vq = __shfl_sync(full, prod, q * NC);
+#pragma unroll
+    for (int u = 1; u < NC; ++u) vq += __shfl_sync(full, prod, q * NC + u);
+    const double mine = per_volume(vq, vol, S.vol, S.uni != 0);
+    const double m2 = mine * mine;
+    double gsq = __shfl_sync(full, m2, 0) + __shfl_sync(full, m2, 1);
+    if (ND == 3) gsq = gsq + __shfl_sync(full, m2, 2);
+    const long long gb = __double_as_longlong(gsq);
+    if (gb == 0 || gb > 0x7ff0000000000000LL) break;
+    const double gni = 1.0 / sqrt(gsq);
+    // this lane's coordinate: max(axis[0], min(axis[-1], p - stepsize * g * gni))
+    double v = p - stepsize * mine * gni;
+    long long kv = zkey(v);
+    const bool nan = (kv < 0 ? -kv : kv) > 0x7ff0000000000000LL;
+    if (!nan && X.klo > kv) {
+      v = X.lo;
+      kv = X.klo;
+    }
+    if (!nan && X.khi < kv) {
+      v = X.hi;
+      kv = X.khi;
+    }
+    p = v;
+    kp = kv;
+    if (lane < ND) ray[count * ND + q] = v;
+    count += 1;
+    if (count >= max_step) {
+      if (lane == 0) status[r] = kMaxStepReached;
+      return;
+    }
+  }
+  if (lane < ND) ray[count * ND + q] = sq;
+  if (lane == 0) {
+    counts[r] = count;
+    status[r] = kOk;
+  }
+}
+
 // Reverse each ray (source first, as ray3d returns ray[count::-1]) and pack
 // the rays back to back.
 template <int ND>
@@ -687,10 +826,21 @@ static int launch_rays(const double* const* axes, const int* n, const double* tt
   }
   if (nrays == 0) return kOk;
   const double dist_min = sqrt_threshold(stepsize);
-  // Four lanes per ray while every ray's group fits on the GPU at once (one
+  // A warp per ray while each ray's warp has an SM sub-partition to itself;
+  // four lanes per ray while every ray's group fits on the GPU at once (one
   // source's receivers); one lane per ray for large batches, which are bound
-  // by throughput rather than by the latency of a step.
-  if ((long long)nrays * 4 <= 64LL * 1024) {
+  // by throughput rather than by the latency of a step.  "ray_lanes" picks
+  // one (32, 4 or 1; honor_grid rays run on one or four lanes).
+  const long long lanes_opt = option_value(kOptRayLanes);
+  const int lanes = lanes_opt > 0 ? (int)lanes_opt
+                                  : ((long long)nrays <= 4LL * sm_count()
+                                         ? 32
+                                         : ((long long)nrays * 4 <= 64LL * 1024 ? 4 : 1));
+  if (lanes == 32 && !honor_grid) {
+    ray_warp_kernel<ND><<<(unsigned)((nrays + 3) / 4), 128, 0, (cudaStream_t)stream>>>(
+        ax, ttgrad, grad_stride, grid_index, ends, nrays, sources, stepsize, dist_min, max_step,
+        rays, counts, status);
+  } else if (lanes >= 4) {
     const long long threads = (long long)nrays * 4;
     const unsigned blocks = (unsigned)((threads + 63) / 64);
     if (!honor_grid)

@@ -61,7 +61,7 @@ int grid_for(long long n, int threads) {
   return (int)blocks;
 }
 
-static long long g_options[kOptCount] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+static long long g_options[kOptCount] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
 
 long long option_value(int opt) { return (opt >= 0 && opt < kOptCount) ? g_options[opt] : -1; }
 
@@ -129,6 +129,11 @@ extern "C" int fteik_set_option(const char* name, long long value) {
     g_options[kOptSweep2dSpec] = value < 0 ? -1 : (value ? 1 : 0);
     return kOk;
   }
+  if (std::strcmp(name, "ray_lanes") == 0) {
+    if (value >= 0 && value != 1 && value != 4 && value != 32) return kInvalidArgument;
+    g_options[kOptRayLanes] = value < 0 ? -1 : value;
+    return kOk;
+  }
   if (std::strcmp(name, "sweep2d_wait_ns") == 0) {
     g_options[kOptSweep2dWaitNs] = value < 0 ? -1 : value;
     return kOk;
@@ -154,6 +159,7 @@ extern "C" int fteik_get_option(const char* name, long long* value) {
   else if (std::strcmp(name, "sweep2d_warp") == 0) *value = g_options[kOptSweep2dWarp];
   else if (std::strcmp(name, "sweep2d_speculate") == 0) *value = g_options[kOptSweep2dSpec];
   else if (std::strcmp(name, "sweep2d_wait_ns") == 0) *value = g_options[kOptSweep2dWaitNs];
+  else if (std::strcmp(name, "ray_lanes") == 0) *value = g_options[kOptRayLanes];
   else return kInvalidArgument;
   return kOk;
 }

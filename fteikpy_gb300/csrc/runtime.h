@@ -43,7 +43,8 @@ enum Option : int {
   kOptSweep2dWarp = 7,  // 2D sweeps: 2 a block per source, 1 a warp, 0 one thread
   kOptSweep2dSpec = 8,  // 2D warp sweeps: 0 turns off the speculated updates (same results)
   kOptSweep2dWaitNs = 9,  // 2D block sweeps: bound of one wait between warps, in ns
-  kOptCount = 10,
+  kOptRayLanes = 10,      // rays: lanes per ray, 32, 4 or 1
+  kOptCount = 11,
 };
 long long option_value(int opt);
 

@@ -65,6 +65,9 @@ int fteik_kernel_timing(int on);
  * "sweep2d_speculate": 0 turns off the warp kernel's speculated updates (each
  * row also evaluated with the previous node's value from before the pass,
  * taken when the chain's actual value has the same bits).
+ * "ray_lanes": lanes per ray of fteik_ray3d / fteik_ray2d: 32 (a warp per
+ * ray; the default up to one ray per SM sub-partition), 4 (the default up to
+ * 16384 rays) or 1 (larger launches); honor_grid rays run on 4 or 1.
  * "sweep2d_wait_ns": the bound, in ns, of each wait between the warps of the
  * block-per-source 2D kernel (default 10 s); a wait that reaches it stops
  * the block and the solve returns FTEIK_DEVICE_WAIT_TIMEOUT.

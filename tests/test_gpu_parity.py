@@ -396,9 +396,11 @@ def test_solve3d_both_coefficient_sources(coef):
         lib.fteik_set_option(b"sweep_coef", -1)
 
 
-def test_rays_with_one_and_four_lanes_per_ray_agree():
-    """Large ray batches run one lane per ray, small ones four (one gradient
-    component per lane): the same rays bit for bit, and the oracle's."""
+def test_rays_with_one_four_and_32_lanes_per_ray_agree():
+    """Large ray batches run one lane per ray, smaller ones four (one axis per
+    lane), one source's receivers a warp per ray: the same rays bit for bit,
+    and the oracle's."""
+    from fteikpy_gb300 import _lib
     from fteikpy_gb300._grid import trace_rays
 
     rng = np.random.default_rng(31)
@@ -413,8 +415,14 @@ def test_rays_with_one_and_four_lanes_per_ray_agree():
     max_dist = 2.0 * sum((n * h) ** 2 for n, h in zip(tt.shape, d)) ** 0.5
     max_step = int(max_dist / 10.0)
     many = trace_rays(3, ax, g, None, ends, src[None], 10.0, max_step, False)
-    few = trace_rays(3, ax, g, None, ends[:400], src[None], 10.0, max_step, False)
-    assert all(np.array_equal(a, b) for a, b in zip(many[:400], few))
+    lib = _lib.load()
+    try:
+        for lanes in (-1, 4, 32):
+            assert lib.fteik_set_option(b"ray_lanes", lanes) == 0
+            few = trace_rays(3, ax, g, None, ends[:400], src[None], 10.0, max_step, False)
+            assert all(np.array_equal(a, b) for a, b in zip(many[:400], few)), lanes
+    finally:
+        lib.fteik_set_option(b"ray_lanes", -1)
     tg_o = O.solve3d(1.0 / v, d, [src], 2, True)[1][0]
     sample = rng.choice(len(ends), 40, replace=False)
     ref = O.raytrace(O.axes(tt.shape, d, np.zeros(3)), tg_o, ends[sample], src, 10.0, max_step,
@@ -436,10 +444,22 @@ def test_rays_with_one_and_four_lanes_per_ray_agree():
         (2, (5.0, 7.0), (-1.0, 2.0), None),
     ],
 )
-def test_rays_bitwise_vs_oracle_on_exact_and_inexact_axes(nd, d, og, stepsize):
+@pytest.mark.parametrize("lanes", [-1, 4, 1])
+def test_rays_bitwise_vs_oracle_on_exact_and_inexact_axes(nd, d, og, stepsize, lanes):
     """Rays (no honor_grid) against the oracle bit for bit, on axes where every
     cell has the same volume and on axes where the volumes differ by
-    rounding."""
+    rounding, with each ray kernel (by default 120 rays run a warp per ray)."""
+    from fteikpy_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.fteik_set_option(b"ray_lanes", lanes) == 0
+    try:
+        _rays_bitwise_case(nd, d, og, stepsize)
+    finally:
+        lib.fteik_set_option(b"ray_lanes", -1)
+
+
+def _rays_bitwise_case(nd, d, og, stepsize):
     rng = np.random.default_rng(17)
     shape = (14, 17, 19)[:nd]
     og = np.array(og)

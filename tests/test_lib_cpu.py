@@ -294,7 +294,8 @@ def test_tuning_options_host_side(lib):
                             (b"sweep2d_keys", (0, 1), ()),
                             (b"sweep2d_warp", (0, 1, 2), (3,)),
                             (b"sweep2d_speculate", (0, 1), ()),
-                            (b"sweep2d_wait_ns", (0, 1000, 10**10), ())):
+                            (b"sweep2d_wait_ns", (0, 1000, 10**10), ()),
+                            (b"ray_lanes", (1, 4, 32), (0, 2, 8, 64))):
         for g in good:
             assert lib.fteik_set_option(name, g) == 0
             assert lib.fteik_get_option(name, ctypes.byref(v)) == 0 and v.value == g

@@ -11,6 +11,10 @@
 //  * comparisons, min and max of doubles run on the integer pipe through an
 //    order-preserving integer key of the bit pattern (exact for all non-NaN
 //    values; -0.0 never arises in these kernels);
+//  * tests that only bound a result (whether a node keeps its value, which
+//    operators cannot win, most plane guards) are decided with float bounds
+//    of the doubles on the integer and FP32 pipes (f_below / f_above), and
+//    fall back to FP64 only where those cannot decide;
 //  * multiplication by 0.5 or 4.0 (exact scalings) edits the exponent field;
 //  * division by a per-launch constant c uses a double-double reciprocal of c
 //    and one Markstein correction step: with y = RN(1/c), a quotient q within
@@ -63,6 +67,34 @@ __device__ __forceinline__ double pmin(double a, double b) {
 }
 __device__ __forceinline__ bool deq(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// ---- float bounds of non-negative doubles --------------------------------------
+//
+// A bound test such as "RN(x + y) <= RN(u + v)" needs no FP64 addition when it
+// can be decided with floats rounded the safe way: f_below(x) <= x <=
+// f_above(x) for every finite x >= 0, and __fadd_rd / __fadd_ru round a float
+// sum down / up, so f_above-sums <= f_below-sums implies the real sums are
+// ordered, and RN keeps that order.  Both bounds are built on the integer
+// pipe from x's high word: its top 20 significand bits (truncated, i.e.
+// rounded down, or plus one unit, which is strictly above x), re-biased from
+// double's exponent (1023) to float's (127).  Below float's normal range
+// f_below is 0 (or a float that is still below x) and f_above the least
+// normal float; above it f_below is the largest finite float and f_above +inf.
+// The callers pass traveltimes and spacing-times-slowness factors, which are
+// >= 0; for a negative x (or -0.0) f_below is -inf and f_above 0, so the
+// bounds hold for every non-NaN x.
+__device__ __forceinline__ float f_below(double x) {
+  const int hi = __double2hiint(x);
+  const int d = (int)((unsigned)hi - (896u << 20));  // wraps only for hi < 0
+  const float f = __int_as_float(min(max(d, 0), (255 << 20) - 1) << 3);
+  return hi < 0 ? -__int_as_float(0x7f800000) : f;
+}
+__device__ __forceinline__ float f_above(double x) {
+  const int hi = __double2hiint(x);
+  const int d = (int)((unsigned)hi - (896u << 20)) + 1;
+  const float f = __int_as_float(min(max(d, 1 << 20), 255 << 20) << 3);
+  return hi < 0 ? 0.0f : f;
 }
 
 // ---- exact power-of-two scalings ---------------------------------------------

@@ -193,10 +193,21 @@ __device__ __forceinline__ double finish3d(double t0, double t1d1, double t1d2, 
 // accepting nodes whose plane guards fail would catch more of them, but the
 // guards' coefficient reads then run for every node and cost more than the
 // extra skips save.)
-__device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, double t1d3,
-                                         double tv, double te, double tn, double tev, double ten,
+// Both tests are decided with float bounds (f_below / f_above, directed
+// float additions), so no FP64 instruction runs: t0 <= RN(tv + z1) follows
+// from f_above(t0) <= f_below(tv) + f_below(z1) rounded down, and
+// RN(t0 + 2^-43 M) <= tev from the rounded-up sum <= f_below(tev).  A test
+// the floats cannot decide (values within about 2^-20 of each other) counts
+// as failed, which only gives up a skip: the update then runs in full.  z1,
+// x1, y1 are the 1D candidates' spacing-times-slowness terms (t1d1 = tv + z1,
+// _fteik3d.py:76-104).
+__device__ __forceinline__ bool keeps_t0(double t0, double z1, double x1, double y1, double tv,
+                                         double te, double tn, double tev, double ten,
                                          double tnv, double tnve) {
-  if (!(dle(t0, t1d1) && dle(t0, t1d2) && dle(t0, t1d3))) return false;
+  const float t0u = f_above(t0);
+  if (!(t0u <= __fadd_rd(f_below(tv), f_below(z1)) && t0u <= __fadd_rd(f_below(te), f_below(x1)) &&
+        t0u <= __fadd_rd(f_below(tn), f_below(y1))))
+    return false;
   // all values are >= 0, so their bit patterns order like the values
   long long m = __double_as_longlong(t0);
   m = max(m, __double_as_longlong(tv));
@@ -207,8 +218,10 @@ __device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, do
   m = max(m, __double_as_longlong(tnv));
   m = max(m, __double_as_longlong(tnve));
   if ((m >> 52) <= 44 || (m >> 52) >= 2047) return false;  // tiny, infinite or NaN
-  const double thr = t0 + __longlong_as_double(m - (43LL << 52));  // t0 + 2^-43 M
-  return dle(thr, tev) && dle(thr, ten) && dle(thr, tnv) && dle(thr, tnve);
+  // t0 + 2^-43 M, rounded up
+  const float thr = __fadd_ru(t0u, f_above(__longlong_as_double(m - (43LL << 52))));
+  return thr <= f_below(tev) && thr <= f_below(ten) && thr <= f_below(tnv) &&
+         thr <= f_below(tnve);
 }
 
 // Operators that provably cannot beat t0, for a node that may change (equal
@@ -229,7 +242,10 @@ __device__ __forceinline__ bool keeps_t0(double t0, double t1d1, double t1d2, do
 // branch record either.  a_zx, a_zy, a_xy: the planes' guard coefficients.
 // Returns the mask of the plane operators (bit P) and of the 3D operator
 // (bit 3) that may be left out; 0 when the bound does not apply (M tiny,
-// infinite or NaN).
+// infinite or NaN).  The sums are bounded with floats rounded the safe way
+// (f_above, f_below, __fadd_ru, __fadd_rd), so a test holds only when the
+// FP64 sums would pass it too, and no FP64 instruction runs; the few tests
+// the floats cannot decide leave their operator in.
 __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double tv, double te,
                                                    double tn, double tev, double ten,
                                                    double tnv, double tnve, double a_zx,
@@ -246,17 +262,20 @@ __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double
   m = max(m, __double_as_longlong(a_zy));
   m = max(m, __double_as_longlong(a_xy));
   if ((m >> 52) <= 44 || (m >> 52) >= 2047) return 0u;
-  const double eps = __longlong_as_double(m - (43LL << 52));  // 2^-43 M
-  const double thr = t0 + eps;
+  const float eps = f_above(__longlong_as_double(m - (43LL << 52)));  // >= 2^-43 M
+  const float thr = __fadd_ru(f_above(t0), eps);                       // >= t0 + 2^-43 M
   const double mx = dmax(dmax(tv, te), tn);
   const bool no3d = dle(t1d, mx);
-  const double thr_mx = mx + eps;
-  const double b_zx = tev + a_zx, b_zy = tnv + a_zy, b_xy = ten + a_xy;
+  const float thr_mx = __fadd_ru(f_above(mx), eps);
+  // <= tev + a_zx, tnv + a_zy, ten + a_xy
+  const float b_zx = __fadd_rd(f_below(tev), f_below(a_zx));
+  const float b_zy = __fadd_rd(f_below(tnv), f_below(a_zy));
+  const float b_xy = __fadd_rd(f_below(ten), f_below(a_xy));
   unsigned dead = 0u;
-  if (dle(thr, b_zx) && (no3d || dle(thr_mx, b_zx))) dead |= 1u;
-  if (dle(thr, b_zy) && (no3d || dle(thr_mx, b_zy))) dead |= 2u;
-  if (dle(thr, b_xy) && (no3d || dle(thr_mx, b_xy))) dead |= 4u;
-  if (dle(thr, tnve)) dead |= 8u;
+  if (thr <= b_zx && (no3d || thr_mx <= b_zx)) dead |= 1u;
+  if (thr <= b_zy && (no3d || thr_mx <= b_zy)) dead |= 2u;
+  if (thr <= b_xy && (no3d || thr_mx <= b_xy)) dead |= 4u;
+  if (thr <= f_below(tnve)) dead |= 8u;
   return dead;
 }
 
@@ -277,6 +296,20 @@ __device__ __forceinline__ bool plane_guard(double u, double v, double a, double
   return dlt(hi, lo + c);
 }
 
+// The same guard decided with float bounds where they suffice: 1 when
+// hi < RN(lo + c) (f_above(hi) < the float sum rounded down, which is a
+// double <= lo + c), 0 when it fails (the rounded-up sum <= f_below(hi)), and
+// -1 when the floats cannot tell (hi and lo + c within about 2^-20 of each
+// other), where the caller runs plane_guard.  No FP64 instruction runs.
+__device__ __forceinline__ int plane_guard_bound(double u, double v, double a, double b) {
+  const bool ul = dlt(u, v), vl = dlt(v, u);
+  const double lo = ul ? u : v, hi = ul ? v : u;
+  const double c = ul ? b : (vl ? a : dmin(a, b));
+  if (f_above(hi) < __fadd_rd(f_below(lo), f_below(c))) return 1;
+  if (__fadd_ru(f_above(lo), f_above(c)) <= f_below(hi)) return 0;
+  return -1;
+}
+
 template <bool GRAD, class CP>
 __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
                                                 double te, double tn, double tev, double ten,
@@ -285,9 +318,16 @@ __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double
                                                 int sy, bool bounds, uint8_t& code) {
   const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
   const double a_zx = c.zxa(), a_zy = c.zya(), a_xy = c.xya();
-  const bool gzx = plane_guard(tv, te, a_zx, c.zxb());
-  const bool gzy = plane_guard(tv, tn, a_zy, c.zyb());
-  const bool gxy = plane_guard(te, tn, a_xy, c.xyb());
+  int gzx = plane_guard_bound(tv, te, a_zx, c.zxb());
+  int gzy = plane_guard_bound(tv, tn, a_zy, c.zyb());
+  int gxy = plane_guard_bound(te, tn, a_xy, c.xyb());
+  // The FP64 guard where the floats cannot decide: rare, so a branch that
+  // the lanes here take together only when one of them needs it.
+  if (__any_sync(__activemask(), (gzx | gzy | gxy) < 0)) {
+    if (gzx < 0) gzx = plane_guard(tv, te, a_zx, c.zxb());
+    if (gzy < 0) gzy = plane_guard(tv, tn, a_zy, c.zyb());
+    if (gxy < 0) gxy = plane_guard(te, tn, a_xy, c.xyb());
+  }
   const unsigned dead =
       bounds ? dead_operators(t0, t1d, tv, te, tn, tev, ten, tnv, tnve, a_zx, a_zy, a_xy) : 0u;
   double t2d1 = kBig, t2d2 = kBig, t2d3 = kBig;
@@ -569,13 +609,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const CoefArraysT<int> ca{C,        i1 + jk,  i0 + j1k,  i0 + jk1,
                                   i1 + j1k, i1 + jk1, i0 + j1k1, i1 + j1k1};
         CoefCells cc{{}, o};
-        double t1d1 = 0.0, t1d2 = 0.0, t1d3 = 0.0;
+        // the 1D candidates' spacing-times-slowness terms (t1d1 = tv + z1 ...)
+        double z1 = 0.0, x1 = 0.0, y1 = 0.0;
         bool go = upd;
         if (upd) {
           if (COEF) {
-            t1d1 = tv + ca.z1();
-            t1d2 = te + ca.x1();
-            t1d3 = tn + ca.y1();
+            z1 = ca.z1();
+            x1 = ca.x1();
+            y1 = ca.y1();
           } else {
             const int im = imax(i - 1, 0), ip = imin(i, NZ - 2);
             const long long iu = (sz > 0 ? im : ip) * NXYc, io = (sz > 0 ? ip : im) * NXYc;
@@ -586,14 +627,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 #pragma unroll
                 for (int c = 0; c < 2; ++c)
                   cc.U[a][b][c] = __ldg(slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
-            t1d1 = tv + cc.z1();
-            t1d2 = te + cc.x1();
-            t1d3 = tn + cc.y1();
+            z1 = cc.z1();
+            x1 = cc.x1();
+            y1 = cc.y1();
           }
-          if (keep_test)
-            go = !keeps_t0(t0, t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve);
+          if (keep_test) go = !keeps_t0(t0, z1, x1, y1, tv, te, tn, tev, ten, tnv, tnve);
         }
         if (__any_sync(0xffffffffu, go) && go) {
+          const double t1d1 = tv + z1, t1d2 = te + x1, t1d3 = tn + y1;
           uint8_t code = 0;
           res = COEF ? node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
                                            ca, o, sz, sx, sy, keep_test != 0, code)
@@ -826,11 +867,13 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
                  __double_as_longlong(ten) == b && __double_as_longlong(tnve) == b);
         }
       }
+      // the 1D candidates' spacing-times-slowness terms (t1d1 = tv + z1 ...)
+      double z1 = 0.0, x1 = 0.0, y1 = 0.0;
       if (go) {
         if (COEF) {
-          t1d1 = tv + ca.z1();
-          t1d2 = te + ca.x1();
-          t1d3 = tn + ca.y1();
+          z1 = ca.z1();
+          x1 = ca.x1();
+          y1 = ca.y1();
         } else {
           const int im = imax(i - 1, 0), ip = imin(i, A.NZ - 2);
           const long long iu = (sz > 0 ? im : ip) * NXYc, io = (sz > 0 ? ip : im) * NXYc;
@@ -841,45 +884,69 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
 #pragma unroll
               for (int c = 0; c < 2; ++c)
                 cc.U[a][b][c] = __ldg(A.slow + (a ? io : iu) + (b ? jo : ju) + (c ? ko : ku));
-          t1d1 = tv + cc.z1();
-          t1d2 = te + cc.x1();
-          t1d3 = tn + cc.y1();
+          z1 = cc.z1();
+          x1 = cc.x1();
+          y1 = cc.y1();
         }
-        if (A.keep_test) go = !keeps_t0(t0, t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve);
+        if (A.keep_test) go = !keeps_t0(t0, z1, x1, y1, tv, te, tn, tev, ten, tnv, tnve);
       }
       unsigned dead = 0u;  // operators that provably cannot beat t0 (dead_operators)
-      if (go) {
-        double a_zx, a_zy, a_xy;
-        if (COEF) {
-          a_zx = ca.zxa();
-          a_zy = ca.zya();
-          a_xy = ca.xya();
-          czx = plane_guard(tv, te, a_zx, ca.zxb());
-          czy = plane_guard(tv, tn, a_zy, ca.zyb());
-          cxy = plane_guard(te, tn, a_xy, ca.xyb());
-        } else {
-          a_zx = cc.zxa();
-          a_zy = cc.zya();
-          a_xy = cc.xya();
-          czx = plane_guard(tv, te, a_zx, cc.zxb());
-          czy = plane_guard(tv, tn, a_zy, cc.zyb());
-          cxy = plane_guard(te, tn, a_xy, cc.xyb());
+      // A warp whose nodes all keep t0 runs no FP64 instruction in this stage.
+      if (__any_sync(0xffffffffu, go)) {
+        double a_zx = 0.0, a_zy = 0.0, a_xy = 0.0;
+        int gzx = 0, gzy = 0, gxy = 0;
+        if (go) {
+          t1d1 = tv + z1;
+          t1d2 = te + x1;
+          t1d3 = tn + y1;
+          if (COEF) {
+            a_zx = ca.zxa();
+            a_zy = ca.zya();
+            a_xy = ca.xya();
+            gzx = plane_guard_bound(tv, te, a_zx, ca.zxb());
+            gzy = plane_guard_bound(tv, tn, a_zy, ca.zyb());
+            gxy = plane_guard_bound(te, tn, a_xy, ca.xyb());
+          } else {
+            a_zx = cc.zxa();
+            a_zy = cc.zya();
+            a_xy = cc.xya();
+            gzx = plane_guard_bound(tv, te, a_zx, cc.zxb());
+            gzy = plane_guard_bound(tv, tn, a_zy, cc.zyb());
+            gxy = plane_guard_bound(te, tn, a_xy, cc.xyb());
+          }
         }
-        if (A.keep_test) {
-          dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,
-                                tnve, a_zx, a_zy, a_xy);
-          czx = czx && !(dead & 1u);
-          czy = czy && !(dead & 2u);
-          cxy = cxy && !(dead & 4u);
+        // the FP64 guard where the floats cannot decide (rare)
+        if (__any_sync(0xffffffffu, (gzx | gzy | gxy) < 0)) {
+          if (COEF) {
+            if (gzx < 0) gzx = plane_guard(tv, te, a_zx, ca.zxb());
+            if (gzy < 0) gzy = plane_guard(tv, tn, a_zy, ca.zyb());
+            if (gxy < 0) gxy = plane_guard(te, tn, a_xy, ca.xyb());
+          } else {
+            if (gzx < 0) gzx = plane_guard(tv, te, a_zx, cc.zxb());
+            if (gzy < 0) gzy = plane_guard(tv, tn, a_zy, cc.zyb());
+            if (gxy < 0) gxy = plane_guard(te, tn, a_xy, cc.xyb());
+          }
         }
-        if (COEF) {
-          if (czx) q_zx = ca.zxq();
-          if (czy) q_zy = ca.zyq();
-          if (cxy) q_xy = ca.xyq();
-        } else {
-          if (czx) q_zx = cc.zxq();
-          if (czy) q_zy = cc.zyq();
-          if (cxy) q_xy = cc.xyq();
+        if (go) {
+          czx = gzx > 0;
+          czy = gzy > 0;
+          cxy = gxy > 0;
+          if (A.keep_test) {
+            dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,
+                                  tnve, a_zx, a_zy, a_xy);
+            czx = czx && !(dead & 1u);
+            czy = czy && !(dead & 2u);
+            cxy = cxy && !(dead & 4u);
+          }
+          if (COEF) {
+            if (czx) q_zx = ca.zxq();
+            if (czy) q_zy = ca.zyq();
+            if (cxy) q_xy = ca.xyq();
+          } else {
+            if (czx) q_zx = cc.zxq();
+            if (czy) q_zy = cc.zyq();
+            if (cxy) q_xy = cc.xyq();
+          }
         }
       }
       {

@@ -27,6 +27,8 @@ SIGNATURES = {
     "fteik_set_option": (_I, [ctypes.c_char_p, _LL]),
     "fteik_last_sweep_ms": (_I, [ctypes.POINTER(ctypes.c_float)]),
     "fteik_fp64_peak": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double), _P]),
+    "fteik_sqrt_rn": (_I, [_P, _LL, _P, _P]),
+    "fteik_div_rn": (_I, [_P, _LL, _D, _P, _P]),
     "fteik3d_workspace_bytes": (_SZ, [_I, _I, _I, _I, _I]),
     "fteik3d_solve": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P]),
     "fteik3d_solve_async": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P]),

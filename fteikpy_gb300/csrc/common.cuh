@@ -16,14 +16,15 @@
 //    of the doubles on the integer and FP32 pipes (f_below / f_above), and
 //    fall back to FP64 only where those cannot decide;
 //  * multiplication by 0.5 or 4.0 (exact scalings) edits the exponent field;
-//  * division by a per-launch constant c uses a double-double reciprocal of c
-//    and one Markstein correction step: with y = RN(1/c), a quotient q within
-//    one ulp of a/c (from the double-double product) and the exact remainder
-//    r = a - c*q (one FMA), RN(q + r*y) is the correctly rounded a/c
-//    (P. Markstein's correction theorem, IBM J. Res. Dev. 34(1), 1990; the
-//    division chapter of Muller et al., Handbook of Floating-Point
-//    Arithmetic). The bitwise tests against the oracle, which divides with
-//    IEEE `/`, check it on every solve.
+//  * division by a constant c > 0 (or a divisor shared by several quotients)
+//    multiplies by y = RN(1/c) and settles the last bit with Tuckerman's
+//    rounding test on the FMA remainder (div_tk, two FP64 instructions), or
+//    corrects a double-double quotient (div_dd, four, fewer registers);
+//  * the square root takes a float seed, a fixed-point Newton step on the
+//    integer pipe, one coupled FP64 Newton step and the same rounding test
+//    (sqrt_rn, four FP64 instructions).
+// Both return IEEE's correctly rounded result, bit for bit; the bitwise tests
+// against the oracle, which uses IEEE `/` and sqrt, check them on every solve.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -97,6 +98,82 @@ __device__ __forceinline__ float f_above(double x) {
   return hi < 0 ? 0.0f : f;
 }
 
+// ---- correctly rounded square root with four FP64 instructions ------------------
+//
+// sqrt_rn(x) returns the same bits as IEEE sqrt (RN(sqrt(x))), which the
+// reference's `x ** 0.5` is, with most of the work off the FP64 pipe:
+//  1. x = x' 2^(2k) with x' in [1, 4) (exponent arithmetic), so sqrt(x) =
+//     sqrt(x') 2^k exactly.
+//  2. y0 = rsqrtf of x' rounded down to float (a relative error of at most
+//     about 2^-21.7: 2^-24 from the truncation, and rsqrtf's documented
+//     2 ulp).
+//  3. One Newton step for 1/sqrt(x'), y1 = y0 (3 - x' y0^2) / 2, in 32- and
+//     64-bit fixed point on the integer pipe: a relative error e1 below
+//     about 2^-28 (the truncations; the step's own term 1.5 e0^2 is ~2^-42).
+//  4. One step of the coupled Newton iteration for sqrt and 1/(2 sqrt)
+//     (P. Markstein, IBM J. Res. Dev. 34(1), 1990): g = RN(x' y1),
+//     h = y1 / 2, r = RN(0.5 - g h), g1 = RN(g + g r).  As g and h come from
+//     the same y1, g (1 + r) = sqrt(x') (1 + eta/2 - 1.5 e1^2 + ...) with
+//     |eta| <= 2^-53 the rounding of g: before its own rounding g1 is within
+//     0.5 + 0.14 ulp of sqrt(x') (ulp = 2^-52, sqrt(x') < 2), so
+//     |g1 - sqrt(x')| < 1.2 ulp.
+//  5. Tuckerman's rounding test: with ulp = 2^-52 (g1 in [1, 2)) every
+//     quantity below is a multiple of ulp^2, so sqrt(x') > g1 + ulp/2 exactly
+//     when d = x' - g1^2 > g1 ulp, and sqrt(x') < g1 - ulp/2 exactly when
+//     d <= -g1 ulp (sqrt is never exactly a midpoint).  d = RN(x' - g1^2) is
+//     one FMA; comparing it with the double u = g1 ulp decides every case
+//     except RN(d) = +-u, where d itself might differ from RN(d).  As g1 is
+//     within 1.5 ulp, the result is g1 - ulp, g1 or g1 + ulp.
+// Zero, subnormal, negative, infinite or NaN inputs, a g1 outside [1, 2) and
+// the RN(d) = +-u case take CUDA's sqrt instead (rare: the last two need
+// x' within an ulp or so of 1 or 4, or sqrt(x') within ~2^-104 of a
+// midpoint).  The kernels' tests compare every result bitwise with the
+// oracle's IEEE sqrt, and a dedicated test compares sqrt_rn with CUDA's sqrt
+// on many millions of inputs, including squares and near-midpoint cases.
+__device__ __forceinline__ double sqrt_fallback(double x) { return sqrt(x); }
+
+__device__ __forceinline__ double sqrt_rn(double x) {
+  const int hx = __double2hiint(x);
+  const unsigned lx = (unsigned)__double2loint(x);
+  const int ex = hx >> 20;  // biased exponent; negative x gives ex < 0
+  const int k = (ex - 1023) >> 1;
+  const int s = (ex - 1023) & 1;  // x' = x 2^-2k in [1, 2) (s = 0) or [2, 4) (s = 1)
+  const unsigned mant = (unsigned)hx & 0xfffffu;
+  // x' in fixed point with 30 fraction bits (truncated), and as a float
+  // rounded down
+  const unsigned M = mant | 0x100000u;
+  const unsigned X = (M << (10 + s)) | (lx >> (22 - s));
+  const float xf = __int_as_float(((127 + s) << 23) | (int)((mant << 3) | (lx >> 29)));
+  const float y0 = rsqrtf(xf);  // in (0.5, 1]
+  // y0 in fixed point with 31 fraction bits (exact: y0 has 24 bits)
+  const int fy = __float_as_int(y0);
+  const unsigned Y = ((unsigned)(fy & 0x7fffff) | 0x800000u) << ((fy >> 23) - 119);
+  // y1 = y0 (3 - x' y0^2) / 2
+  const unsigned P = (unsigned)(((unsigned long long)Y * Y) >> 31);  // y0^2 2^31
+  const unsigned long long Q = (unsigned long long)X * P;             // x' y0^2 2^61
+  const unsigned E = (unsigned)(((3ull << 61) - Q) >> 31);            // (3 - x' y0^2) 2^30
+  const unsigned R = (unsigned)(((unsigned long long)Y * E) >> 32);   // y1 2^30
+  // y1 as a double: R in (2^29, 2^30 (1 + 2^-28)), leading bit 29 or 30
+  const int lz = __clz((int)R);
+  const unsigned frac = (R << lz) << 1;  // the bits after the leading one
+  const double y = __hiloint2double(((1024 - lz) << 20) | (int)(frac >> 12), (int)(frac << 20));
+  const double xs = __hiloint2double(((1023 + s) << 20) | (int)mant, (int)lx);
+  const double g = __dmul_rn(xs, y);
+  const double h = __hiloint2double(__double2hiint(y) - (1 << 20), __double2loint(y));  // y/2
+  const double r = __fma_rn(-g, h, 0.5);
+  const double g1 = __fma_rn(g, r, g);
+  const double d = __fma_rn(-g1, g1, xs);
+  const int hg = __double2hiint(g1);
+  const double u = __hiloint2double(hg - (52 << 20), __double2loint(g1));  // g1 2^-52
+  // |d| against u > 0 by bit patterns; d's sign gives the direction
+  const long long bd = __double_as_longlong(d);
+  const long long ad = bd & 0x7fffffffffffffffLL, bu = __double_as_longlong(u);
+  const bool ok = ex > 0 && ex < 2047 && (hg >> 20) == 1023 && ad != bu;
+  if (!ok) return sqrt_fallback(x);
+  const long long gb = __double_as_longlong(g1) + (ad > bu ? (bd < 0 ? -1 : 1) : 0);
+  return __longlong_as_double(gb + ((long long)k << 52));
+}
+
 // ---- exact power-of-two scalings ---------------------------------------------
 
 // 0.5 * x, exact for zero and for |x| >= 2^-1021 (the callers' precondition,
@@ -111,10 +188,56 @@ __device__ __forceinline__ double times4(double x) {
   return (b & 0x7ff0000000000000LL) ? __longlong_as_double(b + (2LL << 52)) : x;
 }
 
-// ---- correctly rounded division by a per-launch constant -----------------------
+// ---- correctly rounded division with two FP64 instructions ------------------------
+//
+// div_tk(x, c, y) = RN(x / c) for c > 0 given y = RN(1/c), by Tuckerman's
+// rounding test (as sqrt_rn above):
+//  * q0 = RN(x y) is within 1.5 ulp of x/c: x y = (x/c)(1 + e) with
+//    |e| < 2^-53, so |x y - x/c| < ulp(q0) (at most a hair more where x/c
+//    crosses a power of two above q0, which leaves q0 + ulp the right
+//    result), plus half an ulp for the rounding.  RN(x/c) is therefore
+//    q0 - ulp, q0 or q0 + ulp in value.
+//  * x/c > q0 + ulp/2 exactly when the remainder x - c q0 > c ulp/2, and
+//    x/c < q0 - ulp/2 exactly when it is < -c ulp/2; a quotient of two
+//    doubles is never a midpoint (its odd part would exceed 2^53).
+//    rem = RN(x - c q0) is one FMA and c ulp/2 a double (c scaled by a
+//    power of two), and RN keeps the order of each comparison, so they
+//    decide every case but RN(rem) = +-c ulp/2.
+// That case, a q0 that is zero, subnormal, infinite, NaN or a power of two
+// (its lower neighbour is half an ulp away), and a c ulp/2 outside the
+// normal range take the IEEE division.  The bitwise tests against the
+// oracle, which divides with IEEE `/`, check it on every solve, and a
+// dedicated test compares it with IEEE division on many millions of inputs.
+__device__ __forceinline__ double div_tk(double x, double c, double y) {
+  const double q0 = __dmul_rn(x, y);
+  const double rem = __fma_rn(-q0, c, x);
+  const long long bq = __double_as_longlong(q0);
+  const int eq = (int)((bq >> 52) & 0x7ff);
+  const int hc = __double2hiint(c);
+  const int eh = ((hc >> 20) & 0x7ff) + eq - 1076;  // exponent field of c ulp(q0) / 2
+  const double half = __hiloint2double(hc + (eq - 1076) * (1 << 20), __double2loint(c));
+  // |rem| against half > 0 by bit patterns; rem's sign gives the direction
+  const long long br = __double_as_longlong(rem);
+  const long long ar = br & 0x7fffffffffffffffLL, bh = __double_as_longlong(half);
+  const bool ok = eq > 0 && eq < 2047 && (bq & 0xfffffffffffffLL) != 0 && eh > 0 && eh < 2047 &&
+                  ar != bh;
+  if (!ok) return x / c;
+  // one ulp away from zero when rem and q0 have the same sign, towards it
+  // otherwise
+  return __longlong_as_double(bq + (ar > bh ? (((br ^ bq) < 0) ? -1 : 1) : 0));
+}
 
+// ---- division by a per-launch constant --------------------------------------------
+
+// Two ways to divide by a constant c > 0, both giving IEEE's RN(x / c):
+//  * div_by: div_tk above, two FP64 instructions;
+//  * div_dd: a double-double reciprocal hi + lo of c makes q = x hi + x lo
+//    (one FMA) faithful, and one Markstein correction with the exact
+//    remainder rounds it correctly (P. Markstein, IBM J. Res. Dev. 34(1),
+//    1990): four FP64 instructions, but fewer live registers, which is what
+//    the team sweep kernel's operators need (measured faster there).
 struct Recip {
-  double c, hi, lo;  // c, RN(1/c), (1 - c*hi)/c
+  double c, hi, lo;  // c > 0, RN(1/c), (1 - c*hi)/c
 };
 __host__ __device__ inline Recip make_recip(double c) {
   Recip r;
@@ -127,37 +250,26 @@ __host__ __device__ inline Recip make_recip(double c) {
 #endif
   return r;
 }
-// RN(x / c) for finite x (no overflow/underflow), as IEEE division returns.
-__device__ __forceinline__ double div_by(double x, const Recip& r) {
-  double q = __fma_rn(x, r.hi, __dmul_rn(x, r.lo));  // faithful quotient
-  double rem = __fma_rn(-q, r.c, x);                 // exact remainder
-  return __fma_rn(rem, r.hi, q);                     // Markstein correction
+__device__ __forceinline__ double div_dd(double x, const Recip& r) {
+  double q = __fma_rn(x, r.hi, __dmul_rn(x, r.lo));
+  double rem = __fma_rn(-q, r.c, x);
+  return __fma_rn(rem, r.hi, q);
 }
+__device__ __forceinline__ double div_by(double x, const Recip& r) { return div_tk(x, r.c, r.hi); }
 
-// RN(a / b) for several numerators sharing one divisor b: y = RN(1/b) and
-// lo = RN((1 - b*y) * y) make y + lo a reciprocal of b accurate to about
-// 2^-104, so q = a*y + a*lo (one FMA) is faithful, and the same Markstein
-// correction as div_by rounds it correctly.  Numerators that are zero (the
-// quotient keeps their sign), non-finite, or so small that the quotient
-// could leave the normal range take the IEEE division.
+// RN(a / b) for several numerators sharing one divisor b > 0: the reciprocal
+// is taken once.
 struct SharedRecip {
-  double b, y, lo;
+  double b, y;
 };
 __device__ __forceinline__ SharedRecip shared_recip(double b) {
   SharedRecip r;
   r.b = b;
   r.y = 1.0 / b;
-  r.lo = __dmul_rn(__fma_rn(-b, r.y, 1.0), r.y);
   return r;
 }
 __device__ __forceinline__ double div_shared(double a, const SharedRecip& r) {
-  const long long ba = __double_as_longlong(a) & 0x7fffffffffffffffLL;
-  const int ea = (int)(ba >> 52), eb = (int)((__double_as_longlong(r.b) >> 52) & 0x7ff);
-  if (ba == 0) return a;
-  if (ea == 0x7ff || ea - eb < -900 || eb < 64 || eb > 1983) return a / r.b;
-  const double q = __fma_rn(a, r.y, __dmul_rn(a, r.lo));
-  const double rem = __fma_rn(-q, r.b, a);
-  return __fma_rn(rem, r.y, q);
+  return div_tk(a, r.b, r.y);
 }
 
 // ---- misc ------------------------------------------------------------------------

@@ -51,7 +51,7 @@ __device__ __forceinline__ double plane_op(double p, double cp, double q, double
                                            double q4, double prod, const Recip& r) {
   double num = p * cp + q * cq;
   double rad = q4 - prod * (d * d);
-  return div_by(num + sqrt(rad), r);
+  return div_dd(num + sqrt_rn(rad), r);
 }
 
 
@@ -149,7 +149,7 @@ __device__ __forceinline__ double op3d(double tv, double te, double tn, double t
   t3 += o.dx2dy2 * (dac * dac);
   if (!dle(t3, t2)) return kBig;
   double t1 = tb * o.dz2i + ta * o.dx2i + tc * o.dy2i;
-  return div_by(t1 + sqrt(t2 - t3), o.rsum);
+  return div_dd(t1 + sqrt_rn(t2 - t3), o.rsum);
 }
 
 // Minimum with the old value and the branch record, _fteik3d.py:161-200.
@@ -182,6 +182,26 @@ __device__ __forceinline__ double finish3d(double t0, double t1d1, double t1d2, 
   return tnew;
 }
 
+// The bound tests below allow a slack of 2^-43 M, M the largest of their
+// inputs (all >= 0).  mh, the largest of the inputs' high words (which order
+// like the values), bounds M < D(mh + 1) (D(h): the double whose high word is h
+// and low word 0), so slack_above(mh) = D(mh + 1 - 43 * 2^20) as a float is a
+// safe upper bound of 2^-43 M.  A larger slack only makes the tests stricter.
+__device__ __forceinline__ int hi_max8(double a, double b, double c, double d, double e,
+                                       double f, double g, double h) {
+  return max(max(max(__double2hiint(a), __double2hiint(b)), max(__double2hiint(c), __double2hiint(d))),
+             max(max(__double2hiint(e), __double2hiint(f)), max(__double2hiint(g), __double2hiint(h))));
+}
+// The slack bound applies: M neither tiny (exponent field > 44) nor infinite
+// or NaN.
+__device__ __forceinline__ bool slack_applies(int mh) {
+  const int e = mh >> 20;
+  return e > 44 && e < 2047;
+}
+__device__ __forceinline__ float slack_above(int mh) {
+  return f_above(__hiloint2double(mh - (43 << 20), 0));
+}
+
 // True when the node provably keeps t0 in this sweep, on a grid with equal
 // spacings.  There every plane operator's value is its diagonal input plus a
 // non-negative root term (_fteik3d.py:113-117 with dz2i = dx2i: ta + tb =
@@ -200,26 +220,16 @@ __device__ __forceinline__ double finish3d(double t0, double t1d1, double t1d2, 
 // the floats cannot decide (values within about 2^-20 of each other) counts
 // as failed, which only gives up a skip: the update then runs in full.  z1,
 // x1, y1 are the 1D candidates' spacing-times-slowness terms (t1d1 = tv + z1,
-// _fteik3d.py:76-104).
-__device__ __forceinline__ bool keeps_t0(double t0, double z1, double x1, double y1, double tv,
-                                         double te, double tn, double tev, double ten,
+// _fteik3d.py:76-104); mh is hi_max8 of the node's eight values.
+__device__ __forceinline__ bool keeps_t0(double t0, int mh, double z1, double x1, double y1,
+                                         double tv, double te, double tn, double tev, double ten,
                                          double tnv, double tnve) {
   const float t0u = f_above(t0);
   if (!(t0u <= __fadd_rd(f_below(tv), f_below(z1)) && t0u <= __fadd_rd(f_below(te), f_below(x1)) &&
         t0u <= __fadd_rd(f_below(tn), f_below(y1))))
     return false;
-  // all values are >= 0, so their bit patterns order like the values
-  long long m = __double_as_longlong(t0);
-  m = max(m, __double_as_longlong(tv));
-  m = max(m, __double_as_longlong(te));
-  m = max(m, __double_as_longlong(tn));
-  m = max(m, __double_as_longlong(tev));
-  m = max(m, __double_as_longlong(ten));
-  m = max(m, __double_as_longlong(tnv));
-  m = max(m, __double_as_longlong(tnve));
-  if ((m >> 52) <= 44 || (m >> 52) >= 2047) return false;  // tiny, infinite or NaN
-  // t0 + 2^-43 M, rounded up
-  const float thr = __fadd_ru(t0u, f_above(__longlong_as_double(m - (43LL << 52))));
+  if (!slack_applies(mh)) return false;
+  const float thr = __fadd_ru(t0u, slack_above(mh));  // >= t0 + 2^-43 M
   return thr <= f_below(tev) && thr <= f_below(ten) && thr <= f_below(tnv) &&
          thr <= f_below(tnve);
 }
@@ -242,27 +252,18 @@ __device__ __forceinline__ bool keeps_t0(double t0, double z1, double x1, double
 // branch record either.  a_zx, a_zy, a_xy: the planes' guard coefficients.
 // Returns the mask of the plane operators (bit P) and of the 3D operator
 // (bit 3) that may be left out; 0 when the bound does not apply (M tiny,
-// infinite or NaN).  The sums are bounded with floats rounded the safe way
+// infinite or NaN; mh is hi_max8 of the node's eight values).  The sums are
+// bounded with floats rounded the safe way
 // (f_above, f_below, __fadd_ru, __fadd_rd), so a test holds only when the
 // FP64 sums would pass it too, and no FP64 instruction runs; the few tests
 // the floats cannot decide leave their operator in.
-__device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double tv, double te,
-                                                   double tn, double tev, double ten,
+__device__ __forceinline__ unsigned dead_operators(double t0, int mh, double t1d, double tv,
+                                                   double te, double tn, double tev, double ten,
                                                    double tnv, double tnve, double a_zx,
                                                    double a_zy, double a_xy) {
-  long long m = __double_as_longlong(t0);
-  m = max(m, __double_as_longlong(tv));
-  m = max(m, __double_as_longlong(te));
-  m = max(m, __double_as_longlong(tn));
-  m = max(m, __double_as_longlong(tev));
-  m = max(m, __double_as_longlong(ten));
-  m = max(m, __double_as_longlong(tnv));
-  m = max(m, __double_as_longlong(tnve));
-  m = max(m, __double_as_longlong(a_zx));
-  m = max(m, __double_as_longlong(a_zy));
-  m = max(m, __double_as_longlong(a_xy));
-  if ((m >> 52) <= 44 || (m >> 52) >= 2047) return 0u;
-  const float eps = f_above(__longlong_as_double(m - (43LL << 52)));  // >= 2^-43 M
+  mh = max(max(mh, __double2hiint(a_zx)), max(__double2hiint(a_zy), __double2hiint(a_xy)));
+  if (!slack_applies(mh)) return 0u;
+  const float eps = slack_above(mh);                                   // >= 2^-43 M
   const float thr = __fadd_ru(f_above(t0), eps);                       // >= t0 + 2^-43 M
   const double mx = dmax(dmax(tv, te), tn);
   const bool no3d = dle(t1d, mx);
@@ -283,7 +284,7 @@ __device__ __forceinline__ unsigned dead_operators(double t0, double t1d, double
 // (_fteik3d.py:76-104: t1d1 = tv + c.z1() ...), which the caller computes
 // first to test whether the node can change.  With `bounds` (equal
 // spacings), operators that provably cannot beat t0 are left out
-// (dead_operators).
+// (dead_operators; mh is hi_max8 of the node's eight values).
 // A plane operator's guard u < v + a && v < u + b (_fteik3d.py:110,122,134:
 // u, v the two face neighbours, a, b >= 0 the guard's spacing-times-slowness
 // factors) with one addition instead of two.  The clause whose left operand
@@ -313,7 +314,7 @@ __device__ __forceinline__ int plane_guard_bound(double u, double v, double a, d
 template <bool GRAD, class CP>
 __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double t1d3, double tv,
                                                 double te, double tn, double tev, double ten,
-                                                double tnv, double tnve, double t0,
+                                                double tnv, double tnve, double t0, int mh,
                                                 const CP& c, const Ops3& o, int sz, int sx,
                                                 int sy, bool bounds, uint8_t& code) {
   const double t1d = dmin(dmin(t1d1, t1d2), t1d3);
@@ -329,7 +330,8 @@ __device__ __forceinline__ double node_update3d(double t1d1, double t1d2, double
     if (gxy < 0) gxy = plane_guard(te, tn, a_xy, c.xyb());
   }
   const unsigned dead =
-      bounds ? dead_operators(t0, t1d, tv, te, tn, tev, ten, tnv, tnve, a_zx, a_zy, a_xy) : 0u;
+      bounds ? dead_operators(t0, mh, t1d, tv, te, tn, tev, ten, tnv, tnve, a_zx, a_zy, a_xy)
+             : 0u;
   double t2d1 = kBig, t2d2 = kBig, t2d3 = kBig;
   if (gzx && !(dead & 1u)) t2d1 = plane3(0, tv, te, tev, c.zxq(), o);
   if (gzy && !(dead & 2u)) t2d2 = plane3(1, tv, tn, tnv, c.zyq(), o);
@@ -611,6 +613,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         CoefCells cc{{}, o};
         // the 1D candidates' spacing-times-slowness terms (t1d1 = tv + z1 ...)
         double z1 = 0.0, x1 = 0.0, y1 = 0.0;
+        int mh = 0;  // hi_max8 of the node's values, for the bound tests
         bool go = upd;
         if (upd) {
           if (COEF) {
@@ -631,15 +634,18 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             x1 = cc.x1();
             y1 = cc.y1();
           }
-          if (keep_test) go = !keeps_t0(t0, z1, x1, y1, tv, te, tn, tev, ten, tnv, tnve);
+          if (keep_test) {
+            mh = hi_max8(t0, tv, te, tn, tev, ten, tnv, tnve);
+            go = !keeps_t0(t0, mh, z1, x1, y1, tv, te, tn, tev, ten, tnv, tnve);
+          }
         }
         if (__any_sync(0xffffffffu, go) && go) {
           const double t1d1 = tv + z1, t1d2 = te + x1, t1d3 = tn + y1;
           uint8_t code = 0;
           res = COEF ? node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
-                                           ca, o, sz, sx, sy, keep_test != 0, code)
+                                           mh, ca, o, sz, sx, sy, keep_test != 0, code)
                      : node_update3d<GRAD>(t1d1, t1d2, t1d3, tv, te, tn, tev, ten, tnv, tnve, t0,
-                                           cc, o, sz, sx, sy, keep_test != 0, code);
+                                           mh, cc, o, sz, sx, sy, keep_test != 0, code);
           if (!deq(res, t0)) {
             tts[n] = res;
             if (GRAD) recs[n] = code;
@@ -869,6 +875,7 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
       }
       // the 1D candidates' spacing-times-slowness terms (t1d1 = tv + z1 ...)
       double z1 = 0.0, x1 = 0.0, y1 = 0.0;
+      int mh = 0;  // hi_max8 of the node's values, for the bound tests
       if (go) {
         if (COEF) {
           z1 = ca.z1();
@@ -888,7 +895,10 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
           x1 = cc.x1();
           y1 = cc.y1();
         }
-        if (A.keep_test) go = !keeps_t0(t0, z1, x1, y1, tv, te, tn, tev, ten, tnv, tnve);
+        if (A.keep_test) {
+          mh = hi_max8(t0, tv, te, tn, tev, ten, tnv, tnve);
+          go = !keeps_t0(t0, mh, z1, x1, y1, tv, te, tn, tev, ten, tnv, tnve);
+        }
       }
       unsigned dead = 0u;  // operators that provably cannot beat t0 (dead_operators)
       // A warp whose nodes all keep t0 runs no FP64 instruction in this stage.
@@ -932,8 +942,8 @@ __global__ void __launch_bounds__(kTeamWarps * 32, FTEIK_TEAM_MIN_BLOCKS)
           czy = gzy > 0;
           cxy = gxy > 0;
           if (A.keep_test) {
-            dead = dead_operators(t0, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten, tnv,
-                                  tnve, a_zx, a_zy, a_xy);
+            dead = dead_operators(t0, mh, dmin(dmin(t1d1, t1d2), t1d3), tv, te, tn, tev, ten,
+                                  tnv, tnve, a_zx, a_zy, a_xy);
             czx = czx && !(dead & 1u);
             czy = czy && !(dead & 2u);
             cxy = cxy && !(dead & 4u);
@@ -1253,7 +1263,7 @@ __device__ __forceinline__ void grad3d_node_at(const double* tt, const uint8_t* 
     const double d = tq - tt[n - cy];
     g2 = div_by(cy > 0 ? d : -d, o.rdy);
   }
-  const double gn = sqrt(g0 * g0 + g1 * g1 + g2 * g2);
+  const double gn = sqrt_rn(g0 * g0 + g1 * g1 + g2 * g2);
   const long long gb = __double_as_longlong(gn);
   if (gb > 0 && gb <= 0x7ff0000000000000LL) {
     // g /= gn, one correctly rounded quotient per component

@@ -44,11 +44,11 @@ __device__ __forceinline__ int search_right_m1(const double* __restrict__ a, int
 __device__ __forceinline__ double dist3(double x1, double y1, double z1, double x2, double y2,
                                         double z2) {
   const double a = x1 - x2, b = y1 - y2, c = z1 - z2;
-  return sqrt(a * a + b * b + c * c);
+  return sqrt_rn(a * a + b * b + c * c);
 }
 __device__ __forceinline__ double dist2(double x1, double y1, double x2, double y2) {
   const double a = x1 - x2, b = y1 - y2;
-  return sqrt(a * a + b * b);
+  return sqrt_rn(a * a + b * b);
 }
 
 // Cell of a query point inside the axes (the bounds check done by the caller):

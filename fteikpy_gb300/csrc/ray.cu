@@ -399,7 +399,7 @@ __global__ void ray_kernel(Axes ax, const double* ttgrad, long long gstride, con
     // gn = sqrt(gsq) > 0 unless gsq is +0 or NaN (a sum of squares)
     const long long gb = __double_as_longlong(gsq);
     if (gb == 0 || gb > 0x7ff0000000000000LL) break;
-    const double gni = 1.0 / sqrt(gsq);
+    const double gni = 1.0 / sqrt_rn(gsq);
 #pragma unroll
     for (int q = 0; q < ND; ++q) delta[q] = stepsize * gv[q] * gni;
     if (honor_grid) {
@@ -607,7 +607,7 @@ __global__ void ray_axis_kernel(Axes ax, const double* ttgrad, long long gstride
     if (ND == 3) gsq = gsq + gv[ND - 1] * gv[ND - 1];
     const long long gb = __double_as_longlong(gsq);
     if (gb == 0 || gb > 0x7ff0000000000000LL) break;
-    const double gni = 1.0 / sqrt(gsq);
+    const double gni = 1.0 / sqrt_rn(gsq);
     // this lane's coordinate: max(axis[0], min(axis[-1], p - stepsize * g * gni))
     double v = p - stepsize * mine * gni;
     long long kv = zkey(v);
@@ -746,7 +746,7 @@ __global__ void __launch_bounds__(128)
     if (ND == 3) gsq = gsq + __shfl_sync(full, m2, 2);
     const long long gb = __double_as_longlong(gsq);
     if (gb == 0 || gb > 0x7ff0000000000000LL) break;
-    const double gni = 1.0 / sqrt(gsq);
+    const double gni = 1.0 / sqrt_rn(gsq);
     // this lane's coordinate: max(axis[0], min(axis[-1], p - stepsize * g * gni))
     double v = p - stepsize * mine * gni;
     long long kv = zkey(v);

@@ -1,5 +1,7 @@
 // Host-side runtime of the C ABI: error reporting, occupancy-derived launch
 // shapes, and the status word of a solve workspace.
+#include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -197,6 +199,36 @@ extern "C" int fteik_fp64_peak(double* scratch, int nblocks, int iters, double* 
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *flops_per_s = 2.0 * 4.0 * iters * (double)nblocks * 256.0 / (ms * 1e-3);
+  return kOk;
+}
+
+__global__ void sqrt_rn_kernel(const double* x, long long n, double* out) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    out[q] = sqrt_rn(x[q]);
+}
+
+extern "C" int fteik_sqrt_rn(const double* x, long long n, double* out, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !out))) return kInvalidArgument;
+  if (n == 0) return kOk;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  sqrt_rn_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(x, n, out);
+  FTEIK_CHECK(cudaGetLastError());
+  return kOk;
+}
+
+__global__ void div_rn_kernel(const double* x, long long n, double c, double y, double* out) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    out[q] = div_tk(x[q], c, y);
+}
+
+extern "C" int fteik_div_rn(const double* x, long long n, double c, double* out, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !out)) || !(c > 0.0) || !std::isfinite(c)) return kInvalidArgument;
+  if (n == 0) return kOk;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  div_rn_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(x, n, c, 1.0 / c, out);
+  FTEIK_CHECK(cudaGetLastError());
   return kOk;
 }
 

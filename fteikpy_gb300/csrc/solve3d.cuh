@@ -67,7 +67,7 @@ __device__ __forceinline__ double t_ana3(int i, int j, int k, const Ops3& o, con
   double a = o.dz * ((double)i - s.zsa);
   double b = o.dx * ((double)j - s.xsa);
   double c = o.dy * ((double)k - s.ysa);
-  return s.vzero * sqrt(a * a + b * b + c * c);
+  return s.vzero * sqrt_rn(a * a + b * b + c * c);
 }
 __device__ __forceinline__ double t_anad3(int i, int j, int k, const Ops3& o, const Source3& s,
                                           double& tzc, double& txc, double& tyc) {

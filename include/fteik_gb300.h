@@ -77,6 +77,15 @@ int fteik_set_option(const char* name, long long value);
 int fteik_get_option(const char* name, long long* value);
 int fteik_last_sweep_ms(float* ms);
 int fteik_fp64_peak(double* scratch, int nblocks, int iters, double* flops_per_s, void* stream);
+/* Diagnostic (no counterpart in the reference): out[i] = the square root the
+ * kernels use (sqrt_rn, correctly rounded like IEEE sqrt with most of its
+ * work off the FP64 pipe) of the n device doubles x[i], on `stream`. */
+int fteik_sqrt_rn(const double* x, long long n, double* out, void* stream);
+/* Diagnostic (no counterpart in the reference): out[i] = x[i] / c as the
+ * kernels divide by a positive constant (div_tk: a product with RN(1/c) and
+ * Tuckerman's rounding test, correctly rounded like IEEE division), for the n
+ * device doubles x[i], on `stream`.  c must be positive and finite. */
+int fteik_div_rn(const double* x, long long n, double c, double* out, void* stream);
 
 /* ---------------------------------------------------------- model set-up --
  * slowness = 1.0 / velocity, as Eikonal2D/3D.solve does before calling the

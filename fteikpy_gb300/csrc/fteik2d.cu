@@ -57,7 +57,7 @@ __device__ __forceinline__ double t_ana2(int i, int j, double dz, double dx, dou
                                          double xsa, double vzero) {
   double a = dz * ((double)i - zsa);
   double b = dx * ((double)j - xsa);
-  return vzero * sqrt_rn(a * a + b * b);
+  return vzero * sqrt(a * a + b * b);
 }
 __device__ __forceinline__ double t_anad2(int i, int j, double dz, double dx, double zsa,
                                           double xsa, double vzero, double& tzc, double& txc) {
@@ -85,7 +85,7 @@ __device__ double delta2(double t1, double tauv, double taue, double tauev, doub
                  4.0 * ((double)sgntx * txc * dxi * ta + (double)sgntz * tzc * dzi * tb) +
                  4.0 * (vzero * vzero - vref * vref);
   double dpoly = bpoly * bpoly - 4.0 * apoly * cpoly;
-  return dpoly >= 0.0 ? 0.5 * (sqrt_rn(dpoly) - bpoly) / apoly + t0c : t1;
+  return dpoly >= 0.0 ? 0.5 * (sqrt(dpoly) - bpoly) / apoly + t0c : t1;
 }
 
 // Comparisons of the node update.  K = false: IEEE comparisons, which keep
@@ -163,14 +163,14 @@ __device__ __forceinline__ double node_update2d(double* tt, uint8_t* rec, const 
       const double ta = tev + te - tv;
       const double tb = tev - te + tv;
       const double d = ta - tb;
-      t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt_rn(times4(vref * vref) * o.s2 - o.p2 * (d * d)),
+      t2d = div_dd((tb * o.dz2i + ta * o.dx2i) + sqrt(times4(vref * vref) * o.s2 - o.p2 * (d * d)),
                    o.r2);
-    } else if (le2<K>(te - tev, div_by(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, te - tev)) {
-      const double r = div_by(te - tev, o.rdz);
-      t2d = te + o.dx * sqrt_rn(vref * vref - r * r);
-    } else if (le2<K>(tv - tev, div_by(o.dxx * vref, o.rhyp)) && lt2<K>(0.0, tv - tev)) {
-      const double r = div_by(tv - tev, o.rdx);
-      t2d = tv + o.dz * sqrt_rn(vref * vref - r * r);
+    } else if (le2<K>(te - tev, div_dd(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, te - tev)) {
+      const double r = div_dd(te - tev, o.rdz);
+      t2d = te + o.dx * sqrt(vref * vref - r * r);
+    } else if (le2<K>(tv - tev, div_dd(o.dxx * vref, o.rhyp)) && lt2<K>(0.0, tv - tev)) {
+      const double r = div_dd(tv - tev, o.rdx);
+      t2d = tv + o.dz * sqrt(vref * vref - r * r);
     }
   } else {
     // spherical (factored) operator near the source, _fteik2d.py:144-171
@@ -532,12 +532,12 @@ __device__ __forceinline__ double eval_node2d(const Ops2& o, const Source2& sp, 
       const double ta = R.p1 - tv;
       const double tb = R.p2 + tv;
       const double d = ta - tb;
-      t2d = div_by((tb * o.dz2i + ta * o.dx2i) + sqrt_rn(R.x - o.p2 * (d * d)), o.r2);
+      t2d = div_dd((tb * o.dz2i + ta * o.dx2i) + sqrt(R.x - o.p2 * (d * d)), o.r2);
     } else if (f & 2u) {
       t2d = P.t2[q];
     } else if (le2<K>(tv - tev, P.d3[q]) && lt2<K>(0.0, tv - tev)) {
-      const double r = div_by(tv - tev, o.rdx);
-      t2d = tv + o.dz * sqrt_rn(P.vv[q] - r * r);
+      const double r = div_dd(tv - tev, o.rdx);
+      t2d = tv + o.dz * sqrt(P.vv[q] - r * r);
     }
   } else {
     // spherical (factored) operator near the source, _fteik2d.py:144-171
@@ -592,12 +592,12 @@ __device__ __forceinline__ void precompute_row2d(PreT& P, int q, const double* t
   P.te[q] = te;
   P.tev[q] = tev;
   P.vref[q] = vref;
-  P.d3[q] = div_by(o.dxx * vref, o.rhyp);
+  P.d3[q] = div_dd(o.dxx * vref, o.rhyp);
   unsigned f = le2<K>(tev, te) ? 1u : 0u;
   const double dte = te - tev;
-  if (le2<K>(dte, div_by(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, dte)) {
-    const double r = div_by(dte, o.rdz);
-    P.t2[q] = te + o.dx * sqrt_rn(vv - r * r);
+  if (le2<K>(dte, div_dd(o.dzz * vref, o.rhyp)) && lt2<K>(0.0, dte)) {
+    const double r = div_dd(dte, o.rdz);
+    P.t2[q] = te + o.dx * sqrt(vv - r * r);
     f |= 2u;
   }
   P.flags[q] = (unsigned char)f;
@@ -944,7 +944,7 @@ __global__ void grad2d_kernel(const double* tt, const uint8_t* rec, const Source
     const double tq = tt[q];
     if (cz != 0) g0 = (double)cz * (tq - tt[q - (long long)cz * NX]) / dz;
     if (cx != 0) g1 = (double)cx * (tq - tt[q - cx]) / dx;
-    const double gn = sqrt_rn(g0 * g0 + g1 * g1);
+    const double gn = sqrt(g0 * g0 + g1 * g1);
     if (gn > 0.0) {
       g0 /= gn;
       g1 /= gn;

@@ -69,6 +69,14 @@ __device__ __forceinline__ double pmin(double a, double b) {
 __device__ __forceinline__ bool deq(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
 }
+// -x, or x with its sign flipped when `flip`, on the integer pipe (an FP64
+// negation that is not folded into its consumer takes an FP64 instruction).
+__device__ __forceinline__ double dneg(double x) {
+  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+__device__ __forceinline__ double dflip(double x, bool flip) {
+  return __hiloint2double(__double2hiint(x) ^ (flip ? (int)0x80000000 : 0), __double2loint(x));
+}
 
 // ---- float bounds of non-negative doubles --------------------------------------
 //
@@ -121,7 +129,8 @@ __device__ __forceinline__ float f_above(double x) {
 //     quantity below is a multiple of ulp^2, so sqrt(x') > g1 + ulp/2 exactly
 //     when d = x' - g1^2 > g1 ulp, and sqrt(x') < g1 - ulp/2 exactly when
 //     d <= -g1 ulp (sqrt is never exactly a midpoint).  d = RN(x' - g1^2) is
-//     one FMA; comparing it with the double u = g1 ulp decides every case
+//     one FMA (computed as its negation, RN(g1^2 - x'), so that no operand
+//     needs an FP64 negation); comparing it with the double u = g1 ulp decides every case
 //     except RN(d) = +-u, where d itself might differ from RN(d).  As g1 is
 //     within 1.5 ulp, the result is g1 - ulp, g1 or g1 + ulp.
 // Zero, subnormal, negative, infinite or NaN inputs, a g1 outside [1, 2) and
@@ -157,20 +166,25 @@ __device__ __forceinline__ double sqrt_rn(double x) {
   const int lz = __clz((int)R);
   const unsigned frac = (R << lz) << 1;  // the bits after the leading one
   const double y = __hiloint2double(((1024 - lz) << 20) | (int)(frac >> 12), (int)(frac << 20));
-  const double xs = __hiloint2double(((1023 + s) << 20) | (int)mant, (int)lx);
+  // x' and -x', and -y/2, built from bit patterns: an FP64 negation that
+  // the compiler does not fold into an FMA costs a whole FP64 instruction
+  const int hxs = ((1023 + s) << 20) | (int)mant;
+  const double xs = __hiloint2double(hxs, (int)lx);
+  const double nxs = __hiloint2double(hxs | (int)0x80000000, (int)lx);
   const double g = __dmul_rn(xs, y);
-  const double h = __hiloint2double(__double2hiint(y) - (1 << 20), __double2loint(y));  // y/2
-  const double r = __fma_rn(-g, h, 0.5);
+  const double nh = __hiloint2double((__double2hiint(y) - (1 << 20)) | (int)0x80000000,
+                                     __double2loint(y));  // -y/2
+  const double r = __fma_rn(g, nh, 0.5);
   const double g1 = __fma_rn(g, r, g);
-  const double d = __fma_rn(-g1, g1, xs);
+  const double nd = __fma_rn(g1, g1, nxs);  // RN(g1^2 - x') = -RN(x' - g1^2)
   const int hg = __double2hiint(g1);
   const double u = __hiloint2double(hg - (52 << 20), __double2loint(g1));  // g1 2^-52
   // |d| against u > 0 by bit patterns; d's sign gives the direction
-  const long long bd = __double_as_longlong(d);
+  const long long bd = __double_as_longlong(nd);
   const long long ad = bd & 0x7fffffffffffffffLL, bu = __double_as_longlong(u);
   const bool ok = ex > 0 && ex < 2047 && (hg >> 20) == 1023 && ad != bu;
   if (!ok) return sqrt_fallback(x);
-  const long long gb = __double_as_longlong(g1) + (ad > bu ? (bd < 0 ? -1 : 1) : 0);
+  const long long gb = __double_as_longlong(g1) + (ad > bu ? (bd < 0 ? 1 : -1) : 0);
   return __longlong_as_double(gb + ((long long)k << 52));
 }
 
@@ -190,7 +204,7 @@ __device__ __forceinline__ double times4(double x) {
 
 // ---- correctly rounded division with two FP64 instructions ------------------------
 //
-// div_tk(x, c, y) = RN(x / c) for c > 0 given y = RN(1/c), by Tuckerman's
+// div_tk(x, c, nc, y) = RN(x / c) for c > 0 given nc = -c and y = RN(1/c), by Tuckerman's
 // rounding test (as sqrt_rn above):
 //  * q0 = RN(x y) is within 1.5 ulp of x/c: x y = (x/c)(1 + e) with
 //    |e| < 2^-53, so |x y - x/c| < ulp(q0) (at most a hair more where x/c
@@ -208,9 +222,9 @@ __device__ __forceinline__ double times4(double x) {
 // normal range take the IEEE division.  The bitwise tests against the
 // oracle, which divides with IEEE `/`, check it on every solve, and a
 // dedicated test compares it with IEEE division on many millions of inputs.
-__device__ __forceinline__ double div_tk(double x, double c, double y) {
+__device__ __forceinline__ double div_tk(double x, double c, double nc, double y) {
   const double q0 = __dmul_rn(x, y);
-  const double rem = __fma_rn(-q0, c, x);
+  const double rem = __fma_rn(q0, nc, x);  // x - c q0 (nc = -c: no FP64 negation)
   const long long bq = __double_as_longlong(q0);
   const int eq = (int)((bq >> 52) & 0x7ff);
   const int hc = __double2hiint(c);
@@ -237,11 +251,12 @@ __device__ __forceinline__ double div_tk(double x, double c, double y) {
 //    1990): four FP64 instructions, but fewer live registers, which is what
 //    the team sweep kernel's operators need (measured faster there).
 struct Recip {
-  double c, hi, lo;  // c > 0, RN(1/c), (1 - c*hi)/c
+  double c, nc, hi, lo;  // c > 0, -c, RN(1/c), (1 - c*hi)/c
 };
 __host__ __device__ inline Recip make_recip(double c) {
   Recip r;
   r.c = c;
+  r.nc = -c;
   r.hi = 1.0 / c;
 #ifdef __CUDA_ARCH__
   r.lo = __fma_rn(-c, r.hi, 1.0) / c;
@@ -252,24 +267,27 @@ __host__ __device__ inline Recip make_recip(double c) {
 }
 __device__ __forceinline__ double div_dd(double x, const Recip& r) {
   double q = __fma_rn(x, r.hi, __dmul_rn(x, r.lo));
-  double rem = __fma_rn(-q, r.c, x);
+  double rem = __fma_rn(q, r.nc, x);
   return __fma_rn(rem, r.hi, q);
 }
-__device__ __forceinline__ double div_by(double x, const Recip& r) { return div_tk(x, r.c, r.hi); }
+__device__ __forceinline__ double div_by(double x, const Recip& r) {
+  return div_tk(x, r.c, r.nc, r.hi);
+}
 
 // RN(a / b) for several numerators sharing one divisor b > 0: the reciprocal
 // is taken once.
 struct SharedRecip {
-  double b, y;
+  double b, nb, y;
 };
 __device__ __forceinline__ SharedRecip shared_recip(double b) {
   SharedRecip r;
   r.b = b;
+  r.nb = dneg(b);
   r.y = 1.0 / b;
   return r;
 }
 __device__ __forceinline__ double div_shared(double a, const SharedRecip& r) {
-  return div_tk(a, r.b, r.y);
+  return div_tk(a, r.b, r.nb, r.y);
 }
 
 // ---- misc ------------------------------------------------------------------------

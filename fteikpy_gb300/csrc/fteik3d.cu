@@ -122,8 +122,8 @@ __device__ __forceinline__ double plane3(int P, double u, double w, double x, do
                                          const Ops3& o) {
   const bool zx = P == 0;
   // operands picked first, so that each sum is one add sequence for any P
-  const double a1 = zx ? x : u, a2 = zx ? w : -w, a3 = zx ? -u : x;
-  const double b1 = zx ? x : w, b2 = zx ? -w : -u, b3 = zx ? u : x;
+  const double a1 = zx ? x : u, a2 = dflip(w, !zx), a3 = zx ? dneg(u) : x;
+  const double b1 = zx ? x : w, b2 = dneg(zx ? w : u), b3 = zx ? u : x;
   const double ta = (a1 + a2) + a3;
   const double tb = (b1 + b2) + b3;
   const double p = zx ? tb : ta, q = zx ? ta : tb;
@@ -1253,15 +1253,15 @@ __device__ __forceinline__ void grad3d_node_at(const double* tt, const uint8_t* 
   const double tq = tt[n];
   if (cz != 0) {
     const double d = tq - tt[n - cz * NXY];
-    g0 = div_by(cz > 0 ? d : -d, o.rdz);
+    g0 = div_by(dflip(d, cz < 0), o.rdz);
   }
   if (cx != 0) {
     const double d = tq - tt[n - (long long)cx * NY];
-    g1 = div_by(cx > 0 ? d : -d, o.rdx);
+    g1 = div_by(dflip(d, cx < 0), o.rdx);
   }
   if (cy != 0) {
     const double d = tq - tt[n - cy];
-    g2 = div_by(cy > 0 ? d : -d, o.rdy);
+    g2 = div_by(dflip(d, cy < 0), o.rdy);
   }
   const double gn = sqrt_rn(g0 * g0 + g1 * g1 + g2 * g2);
   const long long gb = __double_as_longlong(gn);

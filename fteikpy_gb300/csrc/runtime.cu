@@ -217,17 +217,18 @@ extern "C" int fteik_sqrt_rn(const double* x, long long n, double* out, void* st
   return kOk;
 }
 
-__global__ void div_rn_kernel(const double* x, long long n, double c, double y, double* out) {
+__global__ void div_rn_kernel(const double* x, long long n, double c, double nc, double y,
+                              double* out) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x)
-    out[q] = div_tk(x[q], c, y);
+    out[q] = div_tk(x[q], c, nc, y);
 }
 
 extern "C" int fteik_div_rn(const double* x, long long n, double c, double* out, void* stream) {
   if (n < 0 || (n > 0 && (!x || !out)) || !(c > 0.0) || !std::isfinite(c)) return kInvalidArgument;
   if (n == 0) return kOk;
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
-  div_rn_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(x, n, c, 1.0 / c, out);
+  div_rn_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(x, n, c, -c, 1.0 / c, out);
   FTEIK_CHECK(cudaGetLastError());
   return kOk;
 }

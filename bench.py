@@ -768,7 +768,7 @@ def run_config5(args):
     lib = _lib.load()
     used_budget = budget if budget is not None else int(
         _adjoint.BUDGET_SHARE * torch.cuda.mem_get_info(dev)[0])
-    chunk, _ = _adjoint._chunk_plan(lib, shape, len(src), NSWEEP, used_budget)
+    chunk, group, _ = _adjoint._chunk_plan(lib, shape, len(src), NSWEEP, used_budget)
     g = g.cpu().numpy()
     T = T.detach().cpu().numpy()
     t_obs_h = t_obs.cpu().numpy()
@@ -781,7 +781,7 @@ def run_config5(args):
         "forward_plain_ms": plain, "forward_with_tape_ms": fwd, "adjoint_ms": bwd,
         "adjoint_over_forward": bwd / plain, "forward_plus_adjoint_over_forward": (fwd + bwd) / plain,
         "memory": {"peak_bytes_above_inputs": int(peak_mem), "budget_bytes": used_budget,
-                   "sources_per_chunk": chunk,
+                   "sources_per_chunk": chunk, "sources_per_reverse_group": group,
                    "tape_bytes_per_node_source": lib.fteik3d_tape_bytes(*shape, 1, NSWEEP, 2)
                    / float(np.prod(np.array(shape) + 1))},
     }

@@ -9,8 +9,9 @@ backward pass maps d(loss)/d(receiver traveltimes) to d(loss)/d(velocity).
 The forward solve keeps a tape of every change its sweeps make
 (``fteik3d_solve_tape``), and the backward pass is the exact reverse-mode
 derivative of those sweeps, so it matches finite differences of the solver for
-any ``nsweep``. Sources run in chunks sized to a device-memory budget; a chunk
-whose tape is not kept is solved again in the backward pass.
+any ``nsweep``. Sources run in chunks sized to a device-memory budget, and the
+backward pass in groups of sources; a chunk whose tape is not kept is solved
+again in the backward pass.
 """
 
 import numpy as np
@@ -101,21 +102,37 @@ def _taped_solve(lib, slow, gridsize, src, nsweep, history, workspace):
     _lib.check(rc, "traveltimes")
 
 
+def _halvings(n):
+    """n, then n halved (rounded up) down to 1."""
+    out = [n]
+    while out[-1] > 1:
+        out.append((out[-1] + 1) // 2)
+    return out
+
+
 def _chunk_plan(lib, shape, nsrc, nsweep, budget):
-    """Sources per chunk, so that one chunk's traveltimes, tape, solve and
-    adjoint workspaces fit ``budget`` bytes (at least one source)."""
+    """(k, group, need): sources per forward chunk (one taped solve), sources
+    per group of the reverse pass, and the bytes a chunk's solve plus a
+    group's reverse pass take.
+
+    The forward chunk holds traveltimes, the tape and the solve's workspace
+    (about 48 bytes per node and source); the reverse pass needs 136 more per
+    node and source of its group, but runs group by group over a kept tape
+    (fteik3d_adjoint_part). So the largest chunk is taken whose solve fits
+    beside the largest group that still fits (at least one source each):
+    fewer, larger solves run faster, and the groups only split the reverse
+    pass, whose result does not depend on them."""
     nz, nx, ny = shape
-
-    def need(k):
-        nodes = (nz + 1) * (nx + 1) * (ny + 1)
-        return (8 * nodes * k + lib.fteik3d_workspace_bytes(nz, nx, ny, k, 2)
-                + lib.fteik3d_tape_bytes(nz, nx, ny, k, nsweep, min(HISTORY, max(8 * nsweep - 1, 0)))
-                + lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, k))
-
-    k = nsrc
-    while k > 1 and need(k) > budget:
-        k = (k + 1) // 2
-    return k, need(k)
+    nodes = (nz + 1) * (nx + 1) * (ny + 1)
+    hist = min(HISTORY, max(8 * nsweep - 1, 0))
+    for k in _halvings(nsrc):
+        solve = (8 * nodes * k + lib.fteik3d_workspace_bytes(nz, nx, ny, k, 2)
+                 + lib.fteik3d_tape_bytes(nz, nx, ny, k, nsweep, hist))
+        for g in _halvings(k):
+            need = solve + lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, g)
+            if need <= budget:
+                return k, g, need
+    return 1, 1, need
 
 
 class _Traveltimes(torch.autograd.Function):
@@ -133,24 +150,30 @@ class _Traveltimes(torch.autograd.Function):
         dev = slow.device
         if budget is None:
             budget = int(BUDGET_SHARE * torch.cuda.mem_get_info(dev)[0])
-        k, chunk_bytes = _chunk_plan(lib, slow.shape, nsrc, nsweep, int(budget))
+        k, group, chunk_bytes = _chunk_plan(lib, slow.shape, nsrc, nsweep, int(budget))
+        group_bytes = lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, group)
         axes = _node_axes(slow.shape, gs)
         src_dev = _device.to_device(src)
         rec = _device.to_device(receivers)
         times = torch.empty((nsrc, len(receivers)), dtype=torch.float64, device=dev)
         ws = torch.empty(lib.fteik3d_workspace_bytes(nz, nx, ny, k, 2), dtype=torch.uint8,
                          device=dev)
-        # Keep each chunk's traveltimes and tape for the backward pass while
-        # they fit beside the working set of one more chunk; the backward pass
-        # solves the others again.
-        kept_bytes, chunks = 0, []
+        # Keep the chunks' traveltimes and tapes for the backward pass, from the
+        # first chunk on, while they fit beside the next chunk's solve and one
+        # group's reverse pass; once one is dropped, the later ones are too
+        # (the backward pass solves them again, after the kept ones are freed).
+        kept_bytes, keeping, chunks = 0, True, []
+        solve_bytes = chunk_bytes - group_bytes
         for a in range(0, nsrc, k):
             b = min(a + k, nsrc)
             tt, vzero, tape, h = _taped_solve(lib, slow, gs, src[a:b], nsweep, None, ws)
             times[a:b] = _receiver_times(tt, axes, src_dev[a:b], vzero, rec)
             size = tt.numel() * 8 + tape.numel()
-            if kept_bytes + size + chunk_bytes <= budget:
-                kept_bytes += size
+            after = kept_bytes + size
+            keeping = keeping and after + group_bytes <= budget and (
+                b == nsrc or after + solve_bytes <= budget)
+            if keeping:
+                kept_bytes = after
                 chunks.append((a, b, h, tt, tape))
             else:
                 chunks.append((a, b, h, None, None))
@@ -158,6 +181,7 @@ class _Traveltimes(torch.autograd.Function):
         ctx.save_for_backward(slow, src_dev, rec)
         ctx.src = src
         ctx.chunks = chunks
+        ctx.group = group
         ctx.nsweep = nsweep
         ctx.gridsize = gs
         ctx.axes = axes
@@ -172,7 +196,11 @@ class _Traveltimes(torch.autograd.Function):
         grad_slow = torch.empty_like(slow)
         ax = ctx.axes
         ws = None
+        aws = torch.empty(lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, ctx.group),
+                          dtype=torch.uint8, device=slow.device)
+        first = True
         for c, (a, b, h, tt, tape) in enumerate(ctx.chunks):
+            ctx.chunks[c] = None  # freed once this chunk is done
             k = b - a
             if tt is None:  # not kept: solve this chunk again (same tape, same bits)
                 if ws is None:
@@ -180,17 +208,21 @@ class _Traveltimes(torch.autograd.Function):
                                      dtype=torch.uint8, device=slow.device)
                 tt, _, tape, _ = _taped_solve(lib, slow, ctx.gridsize, ctx.src[a:b], ctx.nsweep,
                                               h, ws)
-            aws = torch.empty(lib.fteik3d_adjoint_workspace_bytes(nz, nx, ny, k),
-                              dtype=torch.uint8, device=slow.device)
-            rc = lib.fteik3d_adjoint(
-                _device.ptr(slow), nz, nx, ny, *ctx.gridsize, k, ctx.nsweep, _device.ptr(tt), h,
-                _device.ptr(tape), tape.numel(), _device.ptr(ax[0]), _device.ptr(ax[1]),
-                _device.ptr(ax[2]), _device.ptr(src_dev[a:b]), _device.ptr(rec), rec.shape[0],
-                _device.ptr(g[a:b]), int(c > 0), _device.ptr(grad_slow), _device.ptr(aws),
-                aws.numel(), SPIN_LIMIT, _device.stream(),
-            )
-            _lib.check(rc, "traveltimes backward")
-            del tt, tape, aws
+            # the reverse pass in groups of sources, the gradient summed on in
+            # source order
+            for g0 in range(0, k, ctx.group):
+                n = min(ctx.group, k - g0)
+                rc = lib.fteik3d_adjoint_part(
+                    _device.ptr(slow), nz, nx, ny, *ctx.gridsize, k, g0, n, ctx.nsweep,
+                    _device.ptr(tt), h, _device.ptr(tape), tape.numel(), _device.ptr(ax[0]),
+                    _device.ptr(ax[1]), _device.ptr(ax[2]), _device.ptr(src_dev[a:b]),
+                    _device.ptr(rec), rec.shape[0], _device.ptr(g[a:b]), int(not first),
+                    _device.ptr(grad_slow), _device.ptr(aws), aws.numel(), SPIN_LIMIT,
+                    _device.stream(),
+                )
+                _lib.check(rc, "traveltimes backward")
+                first = False
+            del tt, tape
         ctx.chunks = None
         # slowness = 1 / velocity, so dL/dv = -dL/ds * s^2
         grad_velocity = -grad_slow * slow * slow
@@ -215,10 +247,12 @@ def traveltimes(velocity, gridsize, sources, receivers, nsweep=2, memory_budget=
         Sweeps of the solve; the gradient is that of this many sweeps.
     memory_budget : int or None
         Device bytes the solve's tapes and workspaces may take (default: 80%
-        of the free device memory). Sources are solved in consecutive chunks
-        that fit it; the tapes of the chunks that do not fit beside the
-        others are dropped after the forward pass and solved again in the
-        backward pass. The gradient's bits do not depend on the chunking.
+        of the free device memory). The reverse pass runs in groups of
+        sources over each solve's tape, and sources are solved in consecutive
+        chunks when one solve of all of them does not fit; the tapes of the
+        chunks that do not fit beside the others are dropped after the
+        forward pass and solved again in the backward pass. The gradient's
+        bits do not depend on the chunking or the grouping.
 
     Returns
     -------

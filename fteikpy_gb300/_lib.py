@@ -58,6 +58,11 @@ SIGNATURES = {
         [_P, _I, _I, _I, _D, _D, _D, _I, _I, _P, _I, _P, _SZ, _P, _P, _P, _P, _P, _I, _P, _I,
          _P, _P, _SZ, _LL, _P],
     ),
+    "fteik3d_adjoint_part": (
+        _I,
+        [_P, _I, _I, _I, _D, _D, _D, _I, _I, _I, _I, _P, _I, _P, _SZ, _P, _P, _P, _P, _P, _I,
+         _P, _I, _P, _P, _SZ, _LL, _P],
+    ),
     "fteik_resample": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "fteik_correlate1d": (_I, [_I, _P, _P, _I, _P, _I, _P, _P]),
     "fteik2d_workspace_bytes": (_SZ, [_I, _I, _I, _I]),

@@ -289,7 +289,7 @@ __device__ __forceinline__ double tape_replaced(const Tape3& P, int src, long lo
     return kBig;
   }
   if (m - 2 < P.H) return __ldg(P.hist + sn * P.H + (m - 2));
-  const unsigned long long key = tape_key(sn, m);
+  const unsigned long long key = tape_key(sn + P.sn0, m);
   unsigned long long h = tape_slot(key, P.mask);
   for (int q = 0; q < kTapeProbes; ++q) {
     const unsigned long long kq = __ldg(P.key + h);
@@ -670,14 +670,34 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
                                const double* grad_tt_rec, int accumulate, double* grad_slow,
                                void* workspace, size_t workspace_bytes, long long spin_limit,
                                void* stream) {
+  return fteik3d_adjoint_part(slow, nz, nx, ny, dz, dx, dy, nsrc, 0, nsrc, nsweep, tt, history,
+                              tape, tape_bytes, ax0, ax1, ax2, sources, receivers, nrec,
+                              grad_tt_rec, accumulate, grad_slow, workspace, workspace_bytes,
+                              spin_limit, stream);
+}
+
+extern "C" int fteik3d_adjoint_part(const double* slow, int nz, int nx, int ny, double dz,
+                                    double dx, double dy, int nsrc_tape, int src0, int nsrc,
+                                    int nsweep, const double* tt_all, int history,
+                                    const void* tape, size_t tape_bytes, const double* ax0,
+                                    const double* ax1, const double* ax2,
+                                    const double* sources_all, const double* receivers, int nrec,
+                                    const double* grad_tt_rec_all, int accumulate,
+                                    double* grad_slow, void* workspace, size_t workspace_bytes,
+                                    long long spin_limit, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
-  if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || nsweep < 0 || nrec < 0 || !slow || !tt ||
-      !tape || !ax0 || !ax1 || !ax2 || !sources ||
-      (nrec > 0 && (!receivers || !grad_tt_rec)) || !grad_slow || !workspace)
+  if (nz < 2 || nx < 2 || ny < 2 || nsrc < 1 || src0 < 0 || nsrc_tape < src0 + nsrc ||
+      nsweep < 0 || nrec < 0 || !slow || !tt_all || !tape || !ax0 || !ax1 || !ax2 ||
+      !sources_all || (nrec > 0 && (!receivers || !grad_tt_rec_all)) || !grad_slow || !workspace)
     return kInvalidArgument;
-  const size_t tape_need = fteik3d_tape_bytes(nz, nx, ny, nsrc, nsweep, history);
+  const size_t tape_need = fteik3d_tape_bytes(nz, nx, ny, nsrc_tape, nsweep, history);
   if (tape_need == 0) return kInvalidArgument;
   if (tape_bytes < tape_need) return kWorkspaceTooSmall;
+  const long long nodes = (long long)(nz + 1) * (nx + 1) * (ny + 1);
+  // this part's sources: src0 .. src0 + nsrc - 1 of the solve
+  const double* tt = tt_all + src0 * nodes;
+  const double* sources = sources_all + 3LL * src0;
+  const double* grad_tt_rec = nrec > 0 ? grad_tt_rec_all + (long long)nrec * src0 : nullptr;
   const AdjLayout L = adj_layout(nz, nx, ny, nsrc);
   if (workspace_bytes < L.total) return kWorkspaceTooSmall;
   char* ws = (char*)workspace;
@@ -697,8 +717,13 @@ extern "C" int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, doubl
   A.nsrc = nsrc;
   A.o = make_ops3(dz, dx, dy);
   const long long N = A.nodes * nsrc;
-  A.tape = tape_at(const_cast<void*>(tape), tape_layout(nz, nx, ny, nsrc, nsweep, history),
+  A.tape = tape_at(const_cast<void*>(tape), tape_layout(nz, nx, ny, nsrc_tape, nsweep, history),
                    nsweep, history);
+  A.tape.code += src0 * nodes * A.tape.E;
+  A.tape.hist += src0 * nodes * A.tape.H;
+  A.tape.init8 += 8LL * src0;
+  A.tape.params += src0;
+  A.tape.sn0 = src0 * nodes;
   A.params = A.tape.params;
   double* vzg = (double*)(ws + L.vzg);
 

@@ -139,6 +139,10 @@ struct Tape3 {
   Source3* params;
   unsigned long long mask;  // table capacity - 1
   int E, H;
+  // Added to a source-node index before it forms a table key: a tape viewed
+  // from its source src0 on (code, hist, init8 and params shifted by src0)
+  // has sn0 = src0 * nodes, so its keys stay those the solve wrote.
+  long long sn0;
 };
 
 struct TapeLayout {
@@ -182,6 +186,7 @@ inline Tape3 tape_at(void* base, const TapeLayout& L, int nsweep, int history) {
   t.mask = L.cap - 1;
   t.E = 8 * nsweep;
   t.H = history;
+  t.sn0 = 0;
   return t;
 }
 

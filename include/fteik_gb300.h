@@ -264,6 +264,22 @@ int fteik3d_adjoint(const double* slow, int nz, int nx, int ny, double dz, doubl
                     const double* sources, const double* receivers, int nrec,
                     const double* grad_tt_rec, int accumulate, double* grad_slow,
                     void* workspace, size_t workspace_bytes, long long spin_limit, void* stream);
+/* fteik3d_adjoint_part: the same reverse pass for the sources src0 ..
+ * src0 + nsrc - 1 of a solve of nsrc_tape sources, from that solve's whole tt,
+ * tape, sources and grad_tt_rec (all indexed from source 0). Its workspace is
+ * fteik3d_adjoint_workspace_bytes(nz, nx, ny, nsrc), for the part only, so a
+ * long solve's reverse pass can run in source groups that fit a memory
+ * budget; with accumulate = 1 after the first group the result is the
+ * whole-solve gradient bit for bit. fteik3d_adjoint is the part src0 = 0,
+ * nsrc = nsrc_tape. (No counterpart in the reference.) */
+int fteik3d_adjoint_part(const double* slow, int nz, int nx, int ny, double dz, double dx,
+                         double dy, int nsrc_tape, int src0, int nsrc, int nsweep,
+                         const double* tt, int history, const void* tape, size_t tape_bytes,
+                         const double* ax0, const double* ax1, const double* ax2,
+                         const double* sources, const double* receivers, int nrec,
+                         const double* grad_tt_rec, int accumulate, double* grad_slow,
+                         void* workspace, size_t workspace_bytes, long long spin_limit,
+                         void* stream);
 
 /* ------------------------------------------------------ model preparation --
  * Replace the SciPy calls of Grid*.resample / Grid*.smooth

@@ -83,16 +83,22 @@ def test_tape_sizes_and_history_limits(lib):
 
 
 def test_adjoint_chunk_plan():
-    """Sources per chunk halve until one chunk's traveltimes, tape and
-    workspaces fit the budget (never below one source)."""
+    """The forward chunk (a taped solve) is the largest that fits beside the
+    largest reverse-pass group that still fits; both halve down to one source."""
     from fteikpy_gb300 import _adjoint
 
     lib = _lib.load()
-    k, need = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, 1 << 50)
-    assert k == 64
-    k2, need2 = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, need // 3)
-    assert k2 == 16 and need2 <= need // 3
-    assert _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, 1)[0] == 1
+    k, g, need = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, 1 << 50)
+    assert (k, g) == (64, 64)
+    # the reverse pass splits first: the solve of all 64 sources stays whole
+    k2, g2, need2 = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, need // 3)
+    assert k2 == 64 and g2 < 64 and need2 <= need // 3
+    k3, g3, need3 = _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, need // 8)
+    assert k3 < 64 and g3 <= k3 and need3 <= need // 8
+    assert _adjoint._chunk_plan(lib, (96, 128, 128), 64, 2, 1)[:2] == (1, 1)
+    # 128x256x256, 64 sources under 40 GB: one solve, reverse pass in groups
+    k4, g4, need4 = _adjoint._chunk_plan(lib, (128, 256, 256), 64, 2, 40 * 10**9)
+    assert k4 == 64 and g4 < 64 and need4 <= 40 * 10**9
     assert _adjoint._history_steps(2) == [2, 6, 15]
     assert _adjoint._history_steps(1) == [2, 6, 7]
     assert _adjoint._history_steps(0) == [0]

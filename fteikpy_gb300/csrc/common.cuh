@@ -178,13 +178,16 @@ __device__ __forceinline__ double sqrt_rn(double x) {
   const double g1 = __fma_rn(g, r, g);
   const double nd = __fma_rn(g1, g1, nxs);  // RN(g1^2 - x') = -RN(x' - g1^2)
   const int hg = __double2hiint(g1);
-  const double u = __hiloint2double(hg - (52 << 20), __double2loint(g1));  // g1 2^-52
-  // |d| against u > 0 by bit patterns; d's sign gives the direction
-  const long long bd = __double_as_longlong(nd);
-  const long long ad = bd & 0x7fffffffffffffffLL, bu = __double_as_longlong(u);
+  // |d| against u = g1 2^-52 > 0 by bit patterns, d's sign giving the
+  // direction.  Both patterns are assembled from 32-bit words: a 64-bit mask
+  // of the sign bit is compiled as an FP64 absolute value (an FP64
+  // instruction).
+  const long long bu = ((long long)(hg - (52 << 20)) << 32) | (unsigned)__double2loint(g1);
+  const int hd = __double2hiint(nd);
+  const long long ad = ((long long)(hd & 0x7fffffff) << 32) | (unsigned)__double2loint(nd);
   const bool ok = ex > 0 && ex < 2047 && (hg >> 20) == 1023 && ad != bu;
   if (!ok) return sqrt_fallback(x);
-  const long long gb = __double_as_longlong(g1) + (ad > bu ? (bd < 0 ? 1 : -1) : 0);
+  const long long gb = __double_as_longlong(g1) + (ad > bu ? (hd < 0 ? 1 : -1) : 0);
   return __longlong_as_double(gb + ((long long)k << 52));
 }
 
@@ -229,16 +232,20 @@ __device__ __forceinline__ double div_tk(double x, double c, double nc, double y
   const int eq = (int)((bq >> 52) & 0x7ff);
   const int hc = __double2hiint(c);
   const int eh = ((hc >> 20) & 0x7ff) + eq - 1076;  // exponent field of c ulp(q0) / 2
-  const double half = __hiloint2double(hc + (eq - 1076) * (1 << 20), __double2loint(c));
-  // |rem| against half > 0 by bit patterns; rem's sign gives the direction
-  const long long br = __double_as_longlong(rem);
-  const long long ar = br & 0x7fffffffffffffffLL, bh = __double_as_longlong(half);
+  // c ulp(q0) / 2 (a power-of-two scaling of c), and |rem| against it by bit
+  // patterns, rem's sign giving the direction; both assembled from 32-bit
+  // words (a 64-bit mask of the sign bit is compiled as an FP64 absolute
+  // value)
+  const long long bh = ((long long)(hc + (eq - 1076) * (1 << 20)) << 32) |
+                       (unsigned)__double2loint(c);
+  const int hr = __double2hiint(rem);
+  const long long ar = ((long long)(hr & 0x7fffffff) << 32) | (unsigned)__double2loint(rem);
   const bool ok = eq > 0 && eq < 2047 && (bq & 0xfffffffffffffLL) != 0 && eh > 0 && eh < 2047 &&
                   ar != bh;
   if (!ok) return x / c;
   // one ulp away from zero when rem and q0 have the same sign, towards it
   // otherwise
-  return __longlong_as_double(bq + (ar > bh ? (((br ^ bq) < 0) ? -1 : 1) : 0));
+  return __longlong_as_double(bq + (ar > bh ? (((hr ^ (int)(bq >> 32)) < 0) ? -1 : 1) : 0));
 }
 
 // ---- division by a per-launch constant --------------------------------------------

@@ -73,9 +73,11 @@ struct Axes {
 // Order key of a non-NaN double in which -0.0 and +0.0 are equal:
 // zkey(a) < zkey(b) <=> a < b.
 __device__ __forceinline__ long long zkey(double x) {
-  const long long b = __double_as_longlong(x);
-  const long long m = b & 0x7fffffffffffffffLL;
-  return b < 0 ? -m : m;
+  // |x|'s pattern from 32-bit words: a 64-bit mask of the sign bit would be
+  // compiled as an FP64 absolute value
+  const int h = __double2hiint(x);
+  const long long m = ((long long)(h & 0x7fffffff) << 32) | (unsigned)__double2loint(x);
+  return h < 0 ? -m : m;
 }
 
 // Per-axis constants of one launch, set up by every block in shared memory.

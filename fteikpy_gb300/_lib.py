@@ -29,6 +29,7 @@ SIGNATURES = {
     "fteik_fp64_peak": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_double), _P]),
     "fteik_sqrt_rn": (_I, [_P, _LL, _P, _P]),
     "fteik_div_rn": (_I, [_P, _LL, _D, _P, _P]),
+    "fteik_recip_rn": (_I, [_P, _LL, _P, _P]),
     "fteik3d_workspace_bytes": (_SZ, [_I, _I, _I, _I, _I]),
     "fteik3d_solve": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P]),
     "fteik3d_solve_async": (_I, [_P, _I, _I, _I, _D, _D, _D, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _LL, _P]),

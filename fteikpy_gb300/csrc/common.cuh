@@ -225,8 +225,10 @@ __device__ __forceinline__ double times4(double x) {
 // normal range take the IEEE division.  The bitwise tests against the
 // oracle, which divides with IEEE `/`, check it on every solve, and a
 // dedicated test compares it with IEEE division on many millions of inputs.
-__device__ __forceinline__ double div_tk(double x, double c, double nc, double y) {
-  const double q0 = __dmul_rn(x, y);
+// The rounding test on a quotient q0 within 1.5 ulp of x / c (c > 0, nc = -c):
+// returns RN(x / c) through `bits`, or false where IEEE division must decide.
+__device__ __forceinline__ bool tk_round(double x, double q0, double c, double nc,
+                                         long long& bits) {
   const double rem = __fma_rn(q0, nc, x);  // x - c q0 (nc = -c: no FP64 negation)
   const long long bq = __double_as_longlong(q0);
   const int eq = (int)((bq >> 52) & 0x7ff);
@@ -240,12 +242,52 @@ __device__ __forceinline__ double div_tk(double x, double c, double nc, double y
                        (unsigned)__double2loint(c);
   const int hr = __double2hiint(rem);
   const long long ar = ((long long)(hr & 0x7fffffff) << 32) | (unsigned)__double2loint(rem);
-  const bool ok = eq > 0 && eq < 2047 && (bq & 0xfffffffffffffLL) != 0 && eh > 0 && eh < 2047 &&
-                  ar != bh;
-  if (!ok) return x / c;
   // one ulp away from zero when rem and q0 have the same sign, towards it
   // otherwise
-  return __longlong_as_double(bq + (ar > bh ? (((hr ^ (int)(bq >> 32)) < 0) ? -1 : 1) : 0));
+  bits = bq + (ar > bh ? (((hr ^ (int)(bq >> 32)) < 0) ? -1 : 1) : 0);
+  return eq > 0 && eq < 2047 && (bq & 0xfffffffffffffLL) != 0 && eh > 0 && eh < 2047 &&
+         ar != bh;
+}
+
+__device__ __forceinline__ double div_tk(double x, double c, double nc, double y) {
+  long long bits;
+  if (!tk_round(x, __dmul_rn(x, y), c, nc, bits)) return x / c;
+  return __longlong_as_double(bits);
+}
+
+// RN(1 / b) for b > 0 (the IEEE reciprocal) with three FP64 instructions:
+// b = b' 2^(e-1023) with b' in [1, 2); a float seed y0 = RN_f(1 / b') from
+// b' rounded down to float (relative error below 2^-22); one Newton step
+// y1 = y0 (2 - b' y0) in fixed point on the integer pipe (below about
+// 2^-28); one in FP64, y2 = y1 + y1 (1 - b' y1) (two FMAs; within
+// 0.5 ulp + 2^-55 of 1/b'); then the rounding test above with x = 1 (one
+// FMA), and the exact scaling by 2^(1023-e).  Zero, subnormal, negative,
+// infinite or NaN b, a b whose reciprocal leaves the normal range, and the
+// test's undecided cases take IEEE division.
+__device__ __forceinline__ double recip_rn(double b) {
+  const int hb = __double2hiint(b);
+  const unsigned lb = (unsigned)__double2loint(b);
+  const int eb = hb >> 20;  // negative b gives eb < 0
+  const unsigned mant = (unsigned)hb & 0xfffffu;
+  const int hbs = (1023 << 20) | (int)mant;
+  const double bs = __hiloint2double(hbs, (int)lb);
+  const double nbs = __hiloint2double(hbs | (int)0x80000000, (int)lb);
+  const float y0 = __frcp_rn(__int_as_float((127 << 23) | (int)((mant << 3) | (lb >> 29))));
+  // y0 in fixed point with 31 fraction bits (exact: y0 has 24 bits, in (0.5, 1])
+  const int fy = __float_as_int(y0);
+  const unsigned Y = ((unsigned)(fy & 0x7fffff) | 0x800000u) << ((fy >> 23) - 119);
+  const unsigned B = 0x80000000u | (mant << 11) | (lb >> 21);          // b' 2^31
+  const unsigned long long T = (unsigned long long)B * Y;               // b' y0 2^62
+  const unsigned E = (unsigned)(((2ull << 62) - T) >> 31);              // (2 - b' y0) 2^31
+  const unsigned R = (unsigned)(((unsigned long long)Y * E) >> 32);     // y1 2^30
+  const int lz = __clz((int)R);
+  const unsigned frac = (R << lz) << 1;
+  const double y1 = __hiloint2double(((1024 - lz) << 20) | (int)(frac >> 12), (int)(frac << 20));
+  const double e = __fma_rn(nbs, y1, 1.0);
+  const double y2 = __fma_rn(y1, e, y1);
+  long long bits;
+  if (!tk_round(1.0, y2, bs, nbs, bits) || eb < 1 || eb > 2043) return 1.0 / b;
+  return __longlong_as_double(bits + (long long)(1023 - eb) * (1LL << 52));
 }
 
 // ---- division by a per-launch constant --------------------------------------------
@@ -290,7 +332,7 @@ __device__ __forceinline__ SharedRecip shared_recip(double b) {
   SharedRecip r;
   r.b = b;
   r.nb = dneg(b);
-  r.y = 1.0 / b;
+  r.y = recip_rn(b);
   return r;
 }
 __device__ __forceinline__ double div_shared(double a, const SharedRecip& r) {

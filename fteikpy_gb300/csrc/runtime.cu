@@ -233,6 +233,21 @@ extern "C" int fteik_div_rn(const double* x, long long n, double c, double* out,
   return kOk;
 }
 
+__global__ void recip_rn_kernel(const double* x, long long n, double* out) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    out[q] = recip_rn(x[q]);
+}
+
+extern "C" int fteik_recip_rn(const double* x, long long n, double* out, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !out))) return kInvalidArgument;
+  if (n == 0) return kOk;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  recip_rn_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(x, n, out);
+  FTEIK_CHECK(cudaGetLastError());
+  return kOk;
+}
+
 extern "C" const char* fteik_version(void) { return "fteik_gb300 0.1.0 (sm_103a)"; }
 
 extern "C" const char* fteik_last_error(void) { return g_last_error; }

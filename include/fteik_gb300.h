@@ -86,6 +86,10 @@ int fteik_sqrt_rn(const double* x, long long n, double* out, void* stream);
  * Tuckerman's rounding test, correctly rounded like IEEE division), for the n
  * device doubles x[i], on `stream`.  c must be positive and finite. */
 int fteik_div_rn(const double* x, long long n, double c, double* out, void* stream);
+/* Diagnostic (no counterpart in the reference): out[i] = 1 / x[i] as the
+ * gradient post-pass takes the reciprocal of a gradient's norm (recip_rn,
+ * correctly rounded like IEEE division), for the n device doubles x[i]. */
+int fteik_recip_rn(const double* x, long long n, double* out, void* stream);
 
 /* ---------------------------------------------------------- model set-up --
  * slowness = 1.0 / velocity, as Eikonal2D/3D.solve does before calling the

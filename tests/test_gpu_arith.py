@@ -140,3 +140,37 @@ def test_div_rn_special_values():
     x = np.concatenate([x, np.ldexp(1.0, np.arange(-1074, 1024)), -np.ldexp(1.0, np.arange(-1074, 1024))])
     for c in DIVISORS:
         _check_div(x, c)
+
+
+def _check_recip(x):
+    lib = _lib.load()
+    xd = torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64)).to(_device.device())
+    out = torch.empty_like(xd)
+    assert lib.fteik_recip_rn(_device.ptr(xd), xd.numel(), _device.ptr(out), _device.stream()) == _lib.OK
+    ref = torch.ones_like(xd) / xd  # IEEE division (tensor by tensor)
+    bad = (out.view(torch.int64) != ref.view(torch.int64)) & ~(torch.isnan(out) & torch.isnan(ref))
+    nbad = int(bad.sum())
+    if nbad:
+        i = int(torch.nonzero(bad)[0])
+        raise AssertionError(f"{nbad} mismatches, e.g. 1/{float(xd[i])!r} = {float(out[i])!r}, "
+                             f"IEEE {float(ref[i])!r}")
+
+
+def test_recip_rn():
+    """The gradient post-pass's reciprocal (recip_rn): random bit patterns
+    over the whole range, gradient-norm-like values, the neighbours of
+    reciprocals of short significands (results next to a double or a
+    midpoint), and the special values."""
+    rng = np.random.default_rng(5)
+    bits = rng.integers(1, 0x7FF0000000000000, size=1 << 24, dtype=np.int64)
+    _check_recip(bits.view(np.float64))
+    _check_recip(10.0 ** rng.uniform(-6.0, 1.0, size=1 << 22))
+    m = rng.integers(1, 1 << 26, size=1 << 20).astype(np.float64)
+    q = np.ldexp(1.0 + rng.integers(0, 1 << 52, size=1 << 20, dtype=np.int64) * 2.0**-52, 0)
+    x = np.concatenate([m, 1.0 / q, 1.0 / (q + 2.0**-53), np.ldexp(m, rng.integers(-300, 300, 1 << 20))])
+    _check_recip(_ulp_neighbours(x, 3))
+    tiny = np.nextafter(0.0, 1.0)
+    s = np.array([0.0, -0.0, tiny, 2.2250738585072014e-308, 1.0, 2.0, 0.5, -1.0, -3.0,
+                  np.finfo(np.float64).max, np.inf, -np.inf, np.nan, 1e-300, 1e300])
+    _check_recip(np.concatenate([s, np.ldexp(1.0, np.arange(-1074, 1024)),
+                                 np.ldexp(1.5, np.arange(-1074, 1023))]))

@@ -52,8 +52,8 @@ BYTES_PER_UPDATE = 25  # slowness + tt read + tt write (8 B each) + 1 B branch r
 # FP64 thread instructions (DADD + DMUL + DFMA, one per active lane) and DRAM
 # bytes read + written. The bench scales both by the updates of the timed
 # launch.
-TEAM_FP64_LANE_OPS_PER_UPDATE = (33837472107 + 14876450935 + 12795162258) / 3221225472
-TEAM_DRAM_BYTES_PER_UPDATE = (84906774272 + 8645403904) / 3221225472
+TEAM_FP64_LANE_OPS_PER_UPDATE = (31704945064 + 14876450935 + 12795162258) / 3221225472
+TEAM_DRAM_BYTES_PER_UPDATE = (84846509568 + 8640589312) / 3221225472
 
 
 def smooth2d(rng, shape, sigma):
